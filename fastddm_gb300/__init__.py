@@ -1,0 +1,18 @@
+"""fastddm_gb300: GB300-native (sm_103a) image-structure-function core for FastDDM.
+
+A drop-in ``core='b200'`` for ``fastddm.ddm(img_seq, lags, mode='fft'|'diff',
+window=...)`` and a device implementation of ``azimuthal_average``.  The
+numerical work runs in hand-written CUDA kernels (``csrc/``) behind the C ABI
+declared in ``include/fddm_b200.h``; PyTorch only supplies device memory and
+streams.
+"""
+
+from ._config import DTYPE, IS_SINGLE_PRECISION
+from ._ddm import ddm, _backend
+from ._ddm_b200 import DdmPlan, ddm_device, ddm_diff_b200, ddm_fft_b200
+from ._fftopt import next_fast_len
+from .azimuthalaverage import AzimuthalAverage, azimuthal_average, azimuthal_average_array
+from .imagestructurefunction import ImageStructureFunction
+from . import lags, mask, window
+
+__version__ = "0.1.0"

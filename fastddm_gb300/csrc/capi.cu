@@ -1,0 +1,110 @@
+// C ABI entry points (declared in include/fddm_b200.h).
+#include <string>
+#include <vector>
+#include <cstring>
+#include "fddm_b200.h"
+#include "fddm_internal.h"
+
+namespace {
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+bool map_dtype(int dtype, int& out) {
+  switch (dtype) {
+    case FDDM_U8: out = fddm::DT_U8; return true;
+    case FDDM_I16: out = fddm::DT_I16; return true;
+    case FDDM_U16: out = fddm::DT_U16; return true;
+    case FDDM_I32: out = fddm::DT_I32; return true;
+    case FDDM_U32: out = fddm::DT_U32; return true;
+    case FDDM_F32: out = fddm::DT_F32; return true;
+    case FDDM_F64: out = fddm::DT_F64; return true;
+    default: return false;  // 64-bit integers are converted to FP64 by the caller
+  }
+}
+
+int run(int mode, const void* img, int dtype, uint64_t length, uint64_t height, uint64_t width,
+        const uint32_t* lags, uint64_t nlags, uint64_t nx, uint64_t ny, uint64_t nt, const double* window,
+        double* out, void* work, size_t work_bytes, int precision, void* stream) {
+  g_last_error.clear();
+  if (!img || !out || (nlags && !lags) || !work) return fail(FDDM_ERR_INVALID, "null pointer argument");
+  fddm::DdmRequest r;
+  r.mode = mode;
+  r.precision = precision;
+  if (precision != FDDM_PREC_FF && precision != FDDM_PREC_F64 && precision != FDDM_PREC_F32)
+    return fail(FDDM_ERR_INVALID, "unknown precision " + std::to_string(precision));
+  if (!map_dtype(dtype, r.dtype)) return fail(FDDM_ERR_INVALID, "unsupported input dtype code " + std::to_string(dtype));
+  r.img = img;
+  r.T = (int64_t)length; r.H = (int64_t)height; r.W = (int64_t)width;
+  r.lags.assign(lags, lags + nlags);
+  r.nx = (int64_t)nx; r.ny = (int64_t)ny; r.nt = (int64_t)nt;
+  r.window = window;
+  r.out = out;
+  r.work = work;
+  r.work_bytes = work_bytes;
+  std::string err;
+  int rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  switch (precision) {
+    case FDDM_PREC_FF: rc = fddm::run_ddm_ff(r, st, err); break;
+    case FDDM_PREC_F64: rc = fddm::run_ddm_f64(r, st, err); break;
+    default: rc = fddm::run_ddm_f32(r, st, err); break;
+  }
+  if (rc != 0) return fail(rc, err);
+  return FDDM_OK;
+}
+}  // namespace
+
+namespace fddm {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+int fail_with(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace fddm
+
+extern "C" {
+
+int fddm_b200_version(void) { return 100; }
+
+const char* fddm_b200_last_error(void) { return g_last_error.c_str(); }
+
+int fddm_b200_workspace_size(int mode, int precision, uint64_t length, uint64_t height, uint64_t width,
+                             uint64_t nlags, uint64_t nx, uint64_t ny, uint64_t nt, int has_window,
+                             size_t* bytes) {
+  g_last_error.clear();
+  if (!bytes) return fail(FDDM_ERR_INVALID, "null pointer argument");
+  if (mode != FDDM_MODE_FFT && mode != FDDM_MODE_DIFF) return fail(FDDM_ERR_INVALID, "unknown mode");
+  if (precision != FDDM_PREC_FF && precision != FDDM_PREC_F64 && precision != FDDM_PREC_F32)
+    return fail(FDDM_ERR_INVALID, "unknown precision " + std::to_string(precision));
+  fddm::DdmRequest r;
+  r.mode = mode;
+  r.precision = precision;
+  r.T = (int64_t)length; r.H = (int64_t)height; r.W = (int64_t)width;
+  r.lags.assign(nlags, 0);  // lag values do not change the layout
+  r.nx = (int64_t)nx; r.ny = (int64_t)ny; r.nt = (int64_t)nt;
+  static const double dummy = 0.0;
+  r.window = has_window ? &dummy : nullptr;
+  fddm::WorkLayout L;
+  std::string err;
+  if (!fddm::plan_layout(r, L, err)) return fail(FDDM_ERR_UNSUPPORTED, err);
+  *bytes = L.total;
+  return FDDM_OK;
+}
+
+int fddm_b200_ddm_fft(const void* d_img_seq, int dtype, uint64_t length, uint64_t height, uint64_t width,
+                      const uint32_t* lags, uint64_t nlags, uint64_t nx, uint64_t ny, uint64_t nt,
+                      const double* d_window, double* d_out, void* d_workspace, size_t workspace_bytes,
+                      int precision, void* stream) {
+  return run(fddm::MODE_FFT, d_img_seq, dtype, length, height, width, lags, nlags, nx, ny, nt, d_window, d_out,
+             d_workspace, workspace_bytes, precision, stream);
+}
+
+int fddm_b200_ddm_diff(const void* d_img_seq, int dtype, uint64_t length, uint64_t height, uint64_t width,
+                       const uint32_t* lags, uint64_t nlags, uint64_t nx, uint64_t ny, const double* d_window,
+                       double* d_out, void* d_workspace, size_t workspace_bytes, int precision, void* stream) {
+  return run(fddm::MODE_DIFF, d_img_seq, dtype, length, height, width, lags, nlags, nx, ny, 0, d_window, d_out,
+             d_workspace, workspace_bytes, precision, stream);
+}
+
+}  // extern "C"

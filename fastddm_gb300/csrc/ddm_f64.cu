@@ -1,0 +1,6 @@
+// Structure-function pipeline, f64 tier (FFT scalar, accumulation scalar = double, double).
+#include "ddm_run.cuh"
+
+namespace fddm {
+int run_ddm_f64(const DdmRequest& r, cudaStream_t st, std::string& err) { return run_ddm_t<double, double>(r, st, err); }
+}  // namespace fddm

@@ -1,0 +1,406 @@
+// Image-structure-function pipeline for one image stack, templated on the
+// FFT scalar S (float, ff or double) and the accumulation scalar A used for
+// the cancellation-critical sums (ff or double).
+//
+// Stage 1  k_rows     frames -> (window) -> r2c FFT along x, two real rows
+//                     packed into one complex transform; output R[t][kx][y].
+// Stage 2  k_cols     R -> c2c FFT along y, x 1/sqrt(nx*ny), written q-major
+//                     to the spectrum F[q][t] with q = fftshift_y(ky)*nkx + kx,
+//                     i.e. already in the output's y-shifted order.
+// Stage 3  k_tfft     per q: mean removal, prefix sums of |F - <F>|^2, FFT
+//                     autocorrelation, combination into D(q, lag), PS, VAR.
+//          k_tdiff    per q: D(q, lag) = <|F(t+lag) - F(t)|^2>_t directly.
+// Frames go through stages 1-2 in chunks so that R stays small.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "fft.cuh"
+
+namespace fddm {
+
+// ---------------------------------------------------------------------------
+// pixel conversion
+// ---------------------------------------------------------------------------
+template <class S, class IN> struct pix;
+template <class IN> struct pix<float, IN> {
+  static __device__ __forceinline__ float get(const IN* p, size_t i) { return (float)p[i]; }
+};
+template <> struct pix<float, double> {
+  static __device__ __forceinline__ float get(const double* p, size_t i) { return __double2float_rn(p[i]); }
+};
+template <class IN> struct pix<double, IN> {
+  static __device__ __forceinline__ double get(const IN* p, size_t i) { return (double)p[i]; }
+};
+template <class IN> struct pix<ff, IN> {  // 8/16-bit integers and float are exact in one float
+  static __device__ __forceinline__ ff get(const IN* p, size_t i) { return {(float)p[i], 0.0f}; }
+};
+template <> struct pix<ff, int32_t> {
+  static __device__ __forceinline__ ff get(const int32_t* p, size_t i) {
+    int32_t v = p[i];
+    float h = __int2float_rn(v);
+    long long d = (long long)v - (long long)h;  // exact, |d| <= 64
+    return {h, (float)d};
+  }
+};
+template <> struct pix<ff, uint32_t> {
+  static __device__ __forceinline__ ff get(const uint32_t* p, size_t i) {
+    uint32_t v = p[i];
+    float h = __uint2float_rn(v);
+    long long d = (long long)v - (long long)h;
+    return {h, (float)d};
+  }
+};
+template <> struct pix<ff, double> {
+  static __device__ __forceinline__ ff get(const double* p, size_t i) { return ff_from_double(p[i]); }
+};
+
+// ---------------------------------------------------------------------------
+// warp / block reductions on scalars of type A
+// ---------------------------------------------------------------------------
+template <class A> __device__ __forceinline__ A shfl_down(A v, int o);
+template <> __device__ __forceinline__ ff shfl_down<ff>(ff v, int o) {
+  return {__shfl_down_sync(0xffffffffu, v.h, o), __shfl_down_sync(0xffffffffu, v.l, o)};
+}
+template <> __device__ __forceinline__ double shfl_down<double>(double v, int o) {
+  return __shfl_down_sync(0xffffffffu, v, o);
+}
+template <class A> __device__ __forceinline__ A shfl_up(A v, int o);
+template <> __device__ __forceinline__ ff shfl_up<ff>(ff v, int o) {
+  return {__shfl_up_sync(0xffffffffu, v.h, o), __shfl_up_sync(0xffffffffu, v.l, o)};
+}
+template <> __device__ __forceinline__ double shfl_up<double>(double v, int o) {
+  return __shfl_up_sync(0xffffffffu, v, o);
+}
+
+template <class A> __device__ __forceinline__ A warp_sum(A v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = sc<A>::add(v, shfl_down(v, o));
+  return v;
+}
+
+// Sum of NV values per thread over the block; result broadcast to all threads.
+// `scratch` holds at least NV * 32 values of A.
+template <class A, int NV> __device__ __forceinline__ void block_sum(A (&v)[NV], A* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) scratch[k * 32 + warp] = v[k];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      A x = lane < nw ? scratch[k * 32 + lane] : sc<A>::zero();
+      x = warp_sum(x);
+      if (lane == 0) scratch[k * 32] = x;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = scratch[k * 32];
+  __syncthreads();
+}
+
+// Exclusive block scan of one value per thread; returns the prefix and the total.
+template <class A> __device__ __forceinline__ A block_exclusive_scan(A v, A* scratch, A& total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  A inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    A u = shfl_up(inc, o);
+    if (lane >= o) inc = sc<A>::add(inc, u);
+  }
+  if (lane == 31) scratch[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    A w = lane < nw ? scratch[lane] : sc<A>::zero();
+    A wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      A u = shfl_up(wi, o);
+      if (lane >= o) wi = sc<A>::add(wi, u);
+    }
+    scratch[32 + lane] = sc<A>::sub(wi, w);  // exclusive warp offsets
+    if (lane == 31) scratch[64] = wi;
+  }
+  __syncthreads();
+  A off = scratch[32 + warp];
+  total = scratch[64];
+  A excl = sc<A>::sub(inc, v);
+  A res = sc<A>::add(off, excl);
+  __syncthreads();
+  return res;
+}
+
+// ---------------------------------------------------------------------------
+// Stage 0: window (FP64) -> S, once per call
+// ---------------------------------------------------------------------------
+template <class S> __global__ void k_window_convert(const double* __restrict__ w, S* __restrict__ out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = sc<S>::from_double(w[i]);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 1: row pass
+// grid (ceil(npairs / pairs_per_block), frames in chunk); dynamic smem pairs*nx*cx<S>
+// ---------------------------------------------------------------------------
+template <class S, class IN>
+__global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
+  const int nx = a.nx, W = a.W, H = a.H;
+  const int npairs = (H + 1) >> 1;
+  const int pair0 = blockIdx.x * a.pairs_per_block;
+  const int np = min(a.pairs_per_block, npairs - pair0);
+  const int tl = blockIdx.y;
+  const size_t t = (size_t)a.t0 + tl;
+  const IN* img = reinterpret_cast<const IN*>(a.img) + t * (size_t)H * W;
+  const S* win = reinterpret_cast<const S*>(a.window_s);
+  const int tid = threadIdx.x, nthr = blockDim.x;
+
+  for (int e = tid; e < np * nx; e += nthr) {
+    const int p = e / nx;
+    const int x = e - p * nx;
+    const int y0 = 2 * (pair0 + p);
+    S va = sc<S>::zero(), vb = sc<S>::zero();
+    if (x < W) {
+      va = pix<S, IN>::get(img, (size_t)y0 * W + x);
+      if (win) va = sc<S>::mul(va, win[(size_t)y0 * W + x]);
+      if (y0 + 1 < H) {
+        vb = pix<S, IN>::get(img, (size_t)(y0 + 1) * W + x);
+        if (win) vb = sc<S>::mul(vb, win[(size_t)(y0 + 1) * W + x]);
+      }
+    }
+    buf[p * nx + x] = {va, vb};
+  }
+  __syncthreads();
+  fft_forward<S>(buf, np, nx, a.px, reinterpret_cast<const cx<S>*>(a.twx), tid, nthr);
+
+  // unpack Z = A + iB into the spectra of the two real rows; write R[tl][k][y]
+  const int nkx = a.nkx;
+  const int ny2 = 2 * np;
+  cx<S>* R = reinterpret_cast<cx<S>*>(a.rbuf) + (size_t)tl * nkx * a.Hpad;
+  for (int e = tid; e < ny2 * nkx; e += nthr) {
+    const int k = e / ny2;
+    const int yl = e - k * ny2;
+    const int p = yl >> 1;
+    const cx<S> zk = buf[p * nx + a.permx[k]];
+    const cx<S> zn = buf[p * nx + a.permx[k == 0 ? 0 : nx - k]];
+    cx<S> v;
+    if ((yl & 1) == 0) {
+      v = {sc<S>::half(sc<S>::add(zk.r, zn.r)), sc<S>::half(sc<S>::sub(zk.i, zn.i))};
+    } else {
+      v = {sc<S>::half(sc<S>::add(zk.i, zn.i)), sc<S>::half(sc<S>::sub(zn.r, zk.r))};
+    }
+    R[(size_t)k * a.Hpad + 2 * pair0 + yl] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stage 2: column pass
+// grid (ceil(nkx / cols_per_block), ceil(frames / frames_per_block))
+// ---------------------------------------------------------------------------
+template <class S>
+__global__ void __launch_bounds__(256) k_cols(SpatialArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
+  const int ny = a.ny, H = a.H, nkx = a.nkx;
+  const int CK = a.cols_per_block, TG = a.frames_per_block;
+  const int kc0 = blockIdx.x * CK;
+  const int tl0 = blockIdx.y * TG;
+  const int nk = min(CK, nkx - kc0);
+  const int ntg = min(TG, a.tc - tl0);
+  const int NB = CK * TG;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const cx<S>* R = reinterpret_cast<const cx<S>*>(a.rbuf);
+
+  for (int e = tid; e < NB * ny; e += nthr) {
+    const int c = e / ny;
+    const int y = e - c * ny;
+    const int tl = c / CK;
+    const int kc = c - tl * CK;
+    cx<S> v = czero<S>();
+    if (kc < nk && tl < ntg && y < H) v = R[((size_t)(tl0 + tl) * nkx + kc0 + kc) * a.Hpad + y];
+    buf[c * ny + y] = v;
+  }
+  __syncthreads();
+  fft_forward<S>(buf, NB, ny, a.py, reinterpret_cast<const cx<S>*>(a.twy), tid, nthr);
+
+  const S norm = sc<S>::cst(a.norm_h, a.norm_l, a.norm_d);
+  cx<S>* F = reinterpret_cast<cx<S>*>(a.spec);
+  const int half = ny >> 1;
+  for (int e = tid; e < NB * ny; e += nthr) {
+    const int tl = e % TG;
+    const int rest = e / TG;
+    const int kc = rest % CK;
+    const int ky = rest / CK;
+    if (tl < ntg && kc < nk) {
+      const cx<S> v = cscale(buf[(tl * CK + kc) * ny + a.permy[ky]], norm);
+      int ys = ky + half;
+      if (ys >= ny) ys -= ny;
+      const size_t q = (size_t)ys * nkx + kc0 + kc;
+      F[q * a.Tpad + a.t0 + tl0 + tl] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// shared per-q statistics: PS, <F>, VAR
+// ---------------------------------------------------------------------------
+template <class S, class A> struct cvt;
+template <> struct cvt<ff, ff> {
+  static __device__ __forceinline__ ff to_acc(ff v) { return v; }
+  static __device__ __forceinline__ ff to_fft(ff v) { return v; }
+};
+template <> struct cvt<float, ff> {
+  static __device__ __forceinline__ ff to_acc(float v) { return {v, 0.0f}; }
+  static __device__ __forceinline__ float to_fft(ff v) { return __fadd_rn(v.h, v.l); }
+};
+template <> struct cvt<double, double> {
+  static __device__ __forceinline__ double to_acc(double v) { return v; }
+  static __device__ __forceinline__ double to_fft(double v) { return v; }
+};
+
+// ---------------------------------------------------------------------------
+// Stage 3 (fft mode)
+// dynamic smem: nt * cx<S>  +  (T + 1) * A  +  96 * A (reduction scratch)
+// ---------------------------------------------------------------------------
+template <class S, class A>
+__global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int T = a.T, nt = a.nt, nl = a.nlags;
+  cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
+  A* pfx = reinterpret_cast<A*>(smem_raw + (size_t)nt * sizeof(cx<S>));
+  A* scratch = pfx + (T + 1);
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const cx<S>* F = reinterpret_cast<const cx<S>*>(a.spec);
+  const cx<S>* tw = reinterpret_cast<const cx<S>*>(a.twt);
+  const A invT = sc<A>::cst(a.invT_h, a.invT_l, a.invT_d);
+  const A invnt = sc<A>::cst(a.invnt_h, a.invnt_l, a.invnt_d);
+  const int chunk = (T + nthr - 1) / nthr;
+
+  for (size_t q = blockIdx.x; q < a.Q; q += gridDim.x) {
+    const cx<S>* src = F + q * a.Tpad;
+    for (int t = tid; t < nt; t += nthr) buf[t] = t < T ? src[t] : czero<S>();
+    __syncthreads();
+
+    // sums of F and |F|^2
+    A v[3] = {sc<A>::zero(), sc<A>::zero(), sc<A>::zero()};
+    for (int t = tid; t < T; t += nthr) {
+      const cx<S> f = buf[t];
+      const A fr = cvt<S, A>::to_acc(f.r), fi = cvt<S, A>::to_acc(f.i);
+      v[0] = sc<A>::add(v[0], fr);
+      v[1] = sc<A>::add(v[1], fi);
+      v[2] = sc<A>::add(v[2], sc<A>::sqsum(fr, fi));
+    }
+    block_sum<A, 3>(v, scratch);
+    const A mr = sc<A>::mul(v[0], invT), mi = sc<A>::mul(v[1], invT);
+    const A ps = sc<A>::mul(v[2], invT);
+    const S msr = cvt<S, A>::to_fft(mr), msi = cvt<S, A>::to_fft(mi);
+
+    // G = F - <F>; prefix sums of |G|^2 over a contiguous chunk per thread
+    const int t_beg = min(T, tid * chunk), t_end = min(T, t_beg + chunk);
+    A run = sc<A>::zero();
+    for (int t = t_beg; t < t_end; ++t) {
+      cx<S> g = buf[t];
+      g.r = sc<S>::sub(g.r, msr);
+      g.i = sc<S>::sub(g.i, msi);
+      buf[t] = g;
+      run = sc<A>::add(run, sc<A>::sqsum(cvt<S, A>::to_acc(g.r), cvt<S, A>::to_acc(g.i)));
+      pfx[t + 1] = run;
+    }
+    A total;
+    const A off = block_exclusive_scan<A>(run, scratch, total);
+    for (int t = t_beg; t < t_end; ++t) pfx[t + 1] = sc<A>::add(pfx[t + 1], off);
+    if (tid == 0) pfx[0] = sc<A>::zero();
+    __syncthreads();
+
+    // autocorrelation via zero-padded FFT: C(tau) = IFFT(|FFT(G)|^2)(tau) / nt
+    fft_forward<S>(buf, 1, nt, a.pt, tw, tid, nthr);
+    for (int k = tid; k < nt; k += nthr) {
+      const cx<S> x = buf[k];
+      buf[k] = {sc<S>::sqsum(x.r, x.i), sc<S>::zero()};
+    }
+    __syncthreads();
+    fft_inverse<S>(buf, 1, nt, a.pt, tw, tid, nthr);
+
+    const A tot = pfx[T];
+    for (int l = tid; l < nl; l += nthr) {
+      const int tau = a.lags[l];
+      const A c = sc<A>::mul(cvt<S, A>::to_acc(buf[tau].r), invnt);
+      // S1 + S2 - 2 C = pfx[T - tau] + (pfx[T] - pfx[tau]) - 2 C
+      A num = sc<A>::add(pfx[T - tau], sc<A>::sub(tot, pfx[tau]));
+      num = sc<A>::sub(num, sc<A>::add(c, c));
+      a.out[(size_t)l * a.Q + q] = sc<A>::to_double(num) * a.rcp[l];
+    }
+    if (tid == 0) {
+      a.out[(size_t)nl * a.Q + q] = sc<A>::to_double(ps);
+      a.out[(size_t)(nl + 1) * a.Q + q] = sc<A>::to_double(sc<A>::mul(tot, invT));
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stage 3 (diff mode)
+// dynamic smem: T * cx<S> + 96 * A
+// ---------------------------------------------------------------------------
+template <class S, class A>
+__global__ void __launch_bounds__(512) k_tdiff(TemporalArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int T = a.T, nl = a.nlags;
+  cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
+  A* scratch = reinterpret_cast<A*>(smem_raw + (size_t)T * sizeof(cx<S>));
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
+  const cx<S>* F = reinterpret_cast<const cx<S>*>(a.spec);
+  const A invT = sc<A>::cst(a.invT_h, a.invT_l, a.invT_d);
+
+  for (size_t q = blockIdx.x; q < a.Q; q += gridDim.x) {
+    const cx<S>* src = F + q * a.Tpad;
+    for (int t = tid; t < T; t += nthr) buf[t] = src[t];
+    __syncthreads();
+
+    A v[3] = {sc<A>::zero(), sc<A>::zero(), sc<A>::zero()};
+    for (int t = tid; t < T; t += nthr) {
+      const cx<S> f = buf[t];
+      const A fr = cvt<S, A>::to_acc(f.r), fi = cvt<S, A>::to_acc(f.i);
+      v[0] = sc<A>::add(v[0], fr);
+      v[1] = sc<A>::add(v[1], fi);
+      v[2] = sc<A>::add(v[2], sc<A>::sqsum(fr, fi));
+    }
+    block_sum<A, 3>(v, scratch);
+    const A mr = sc<A>::mul(v[0], invT), mi = sc<A>::mul(v[1], invT);
+    const A ps = sc<A>::mul(v[2], invT);
+    A w[1] = {sc<A>::zero()};
+    for (int t = tid; t < T; t += nthr) {
+      const cx<S> f = buf[t];
+      const A gr = sc<A>::sub(cvt<S, A>::to_acc(f.r), mr);
+      const A gi = sc<A>::sub(cvt<S, A>::to_acc(f.i), mi);
+      w[0] = sc<A>::add(w[0], sc<A>::sqsum(gr, gi));
+    }
+    block_sum<A, 1>(w, scratch);
+
+    for (int l = warp; l < nl; l += nw) {
+      const int tau = a.lags[l];
+      A acc = sc<A>::zero();
+      for (int t = lane; t < T - tau; t += 32) {
+        const cx<S> f1 = buf[t + tau], f0 = buf[t];
+        const A dr = sc<A>::sub(cvt<S, A>::to_acc(f1.r), cvt<S, A>::to_acc(f0.r));
+        const A di = sc<A>::sub(cvt<S, A>::to_acc(f1.i), cvt<S, A>::to_acc(f0.i));
+        acc = sc<A>::add(acc, sc<A>::sqsum(dr, di));
+      }
+      acc = warp_sum(acc);
+      if (lane == 0) a.out[(size_t)l * a.Q + q] = sc<A>::to_double(acc) * a.rcp[l];
+    }
+    if (tid == 0) {
+      a.out[(size_t)nl * a.Q + q] = sc<A>::to_double(ps);
+      a.out[(size_t)(nl + 1) * a.Q + q] = sc<A>::to_double(sc<A>::mul(w[0], invT));
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace fddm

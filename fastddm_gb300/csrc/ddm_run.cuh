@@ -1,0 +1,156 @@
+// Host-side driver of the structure-function pipeline for one precision tier.
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include "ddm_impl.cuh"
+
+namespace fddm {
+
+template <class S> struct tier_kind;
+template <> struct tier_kind<ff> { static constexpr int v = 0; };
+template <> struct tier_kind<double> { static constexpr int v = 1; };
+template <> struct tier_kind<float> { static constexpr int v = 2; };
+
+inline void split_ff(double d, float& h, float& l) {
+  h = (float)d;
+  l = (float)(d - (double)h);
+}
+
+constexpr size_t kMaxDynSmem = 232448;  // 227 KB opt-in limit per CTA on sm_100-class parts
+
+template <class K> inline cudaError_t allow_smem(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <class S, class A>
+size_t temporal_smem(int mode, int T, int nt) {
+  if (mode == MODE_FFT) return (size_t)nt * sizeof(cx<S>) + (size_t)(T + 1) * sizeof(A) + 96 * sizeof(A);
+  return (size_t)T * sizeof(cx<S>) + 96 * sizeof(A);
+}
+
+template <class S, class IN>
+cudaError_t launch_rows(const SpatialArgs& a, dim3 grid, size_t smem, cudaStream_t st) {
+  cudaError_t e = allow_smem(k_rows<S, IN>, smem);
+  if (e != cudaSuccess) return e;
+  k_rows<S, IN><<<grid, 256, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t dispatch_rows(int dtype, const SpatialArgs& a, dim3 grid, size_t smem, cudaStream_t st) {
+  switch (dtype) {
+    case DT_U8: return launch_rows<S, uint8_t>(a, grid, smem, st);
+    case DT_I16: return launch_rows<S, int16_t>(a, grid, smem, st);
+    case DT_U16: return launch_rows<S, uint16_t>(a, grid, smem, st);
+    case DT_I32: return launch_rows<S, int32_t>(a, grid, smem, st);
+    case DT_U32: return launch_rows<S, uint32_t>(a, grid, smem, st);
+    case DT_F32: return launch_rows<S, float>(a, grid, smem, st);
+    case DT_F64: return launch_rows<S, double>(a, grid, smem, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// Returns 0 on success, else an FDDM status code with `err` filled in.
+template <class S, class A>
+int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
+  WorkLayout L;
+  if (!plan_layout(r, L, err)) return 4;
+  if (r.work_bytes < L.total) {
+    err = "workspace too small: need " + std::to_string(L.total) + " bytes, got " + std::to_string(r.work_bytes);
+    return 2;
+  }
+  const int kind = tier_kind<S>::v;
+  const int T = (int)r.T, H = (int)r.H, W = (int)r.W, nx = (int)r.nx, ny = (int)r.ny;
+  const int nkx = nx / 2 + 1;
+  const size_t Q = (size_t)ny * nkx;
+  const int nl = (int)r.lags.size();
+  unsigned char* ws = static_cast<unsigned char*>(r.work);
+
+  FftTables tx, ty, tt;
+  if (!get_tables(nx, kind, tx, err) || !get_tables(ny, kind, ty, err)) return 3;
+  if (r.mode == MODE_FFT && !get_tables((int)r.nt, kind, tt, err)) return 3;
+
+  cudaError_t ce;
+  // window in the FFT scalar type
+  const void* win_s = nullptr;
+  if (r.window) {
+    S* w = reinterpret_cast<S*>(ws + L.win_off);
+    const size_t n = (size_t)H * W;
+    k_window_convert<S><<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, st>>>(r.window, w, n);
+    if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+    win_s = w;
+  }
+  // lags and reciprocal normalisations
+  std::vector<double> rcp(nl);
+  for (int l = 0; l < nl; ++l) rcp[l] = 1.0 / (double)(T - r.lags[l]);
+  int* d_lags = reinterpret_cast<int*>(ws + L.lags_off);
+  double* d_rcp = reinterpret_cast<double*>(ws + L.rcp_off);
+  if (nl > 0) {
+    if ((ce = cudaMemcpyAsync(d_lags, r.lags.data(), nl * sizeof(int), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(d_rcp, rcp.data(), nl * sizeof(double), cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+      err = cudaGetErrorString(ce);
+      return 3;
+    }
+  }
+
+  // stages 1-2 over frame chunks
+  SpatialArgs sa{};
+  sa.img = r.img;
+  sa.window_s = win_s;
+  sa.T = T; sa.H = H; sa.W = W; sa.nx = nx; sa.ny = ny; sa.nkx = nkx; sa.Hpad = L.Hpad;
+  sa.Tpad = L.Tpad;
+  sa.pairs_per_block = L.pairs_per_block;
+  sa.cols_per_block = L.cols_per_block;
+  sa.frames_per_block = L.frames_per_block;
+  sa.px = tx.plan; sa.py = ty.plan;
+  sa.twx = tx.tw; sa.twy = ty.tw; sa.permx = tx.perm; sa.permy = ty.perm;
+  sa.rbuf = ws + L.rbuf_off;
+  sa.spec = ws + L.spec_off;
+  const double norm = 1.0 / std::sqrt((double)nx * (double)ny);
+  split_ff(norm, sa.norm_h, sa.norm_l);
+  sa.norm_d = norm;
+  const int npairs = (H + 1) / 2;
+  const size_t smem_rows = (size_t)L.pairs_per_block * nx * sizeof(cx<S>);
+  const size_t smem_cols = (size_t)L.cols_per_block * L.frames_per_block * ny * sizeof(cx<S>);
+  if ((ce = allow_smem(k_cols<S>, smem_cols)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+  for (int t0 = 0; t0 < T; t0 += L.chunk) {
+    sa.t0 = t0;
+    sa.tc = std::min(L.chunk, T - t0);
+    dim3 gr((npairs + L.pairs_per_block - 1) / L.pairs_per_block, sa.tc);
+    if ((ce = dispatch_rows<S>(r.dtype, sa, gr, smem_rows, st)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+    dim3 gc((nkx + L.cols_per_block - 1) / L.cols_per_block, (sa.tc + L.frames_per_block - 1) / L.frames_per_block);
+    k_cols<S><<<gc, 256, smem_cols, st>>>(sa);
+    if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+  }
+
+  // stage 3
+  TemporalArgs ta{};
+  ta.spec = ws + L.spec_off;
+  ta.Q = Q; ta.Tpad = L.Tpad; ta.T = T; ta.nt = (int)r.nt; ta.nlags = nl;
+  if (r.mode == MODE_FFT) { ta.pt = tt.plan; ta.twt = tt.tw; }
+  ta.lags = d_lags; ta.rcp = d_rcp; ta.out = r.out;
+  split_ff(1.0 / (double)T, ta.invT_h, ta.invT_l); ta.invT_d = 1.0 / (double)T;
+  if (r.mode == MODE_FFT) { split_ff(1.0 / (double)r.nt, ta.invnt_h, ta.invnt_l); ta.invnt_d = 1.0 / (double)r.nt; }
+  const size_t smem_t = temporal_smem<S, A>(r.mode, T, (int)r.nt);
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int threads = 512;
+  if (r.mode == MODE_FFT) {
+    if ((ce = allow_smem(k_tfft<S, A>, smem_t)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tfft<S, A>, threads, smem_t);
+  } else {
+    if ((ce = allow_smem(k_tdiff<S, A>, smem_t)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tdiff<S, A>, threads, smem_t);
+  }
+  if (occ < 1) { err = "temporal kernel does not fit on an SM (shared memory " + std::to_string(smem_t) + " B)"; return 4; }
+  const unsigned grid = (unsigned)std::min<size_t>(Q, (size_t)occ * nsm);
+  if (r.mode == MODE_FFT) k_tfft<S, A><<<grid, threads, smem_t, st>>>(ta);
+  else k_tdiff<S, A><<<grid, threads, smem_t, st>>>(ta);
+  if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+  return 0;
+}
+
+}  // namespace fddm

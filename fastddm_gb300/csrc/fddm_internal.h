@@ -1,0 +1,105 @@
+// Internal host/device structures shared by the kernels and the C ABI layer.
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+
+namespace fddm {
+
+constexpr int kMaxPass = 24;
+
+struct FftPlan {
+  int n;                // transform length
+  int npass;            // number of passes
+  int radix[kMaxPass];  // radix of pass s
+  int block[kMaxPass];  // block size M_s at pass s (M_0 = n)
+};
+
+struct SpatialArgs {
+  const void* img;       // (T, H, W) frames, input dtype
+  const void* window_s;  // (H, W) window in the FFT scalar type, or null
+  int T, H, W, nx, ny, nkx, Hpad;
+  int t0, tc;            // first frame and number of frames of this chunk
+  int Tpad;              // spectrum row stride (elements)
+  int pairs_per_block, cols_per_block, frames_per_block;
+  FftPlan px, py;
+  const void* twx;
+  const void* twy;
+  const int* permx;
+  const int* permy;
+  void* rbuf;            // (tc, nkx, Hpad) row-pass output
+  void* spec;            // (Q, Tpad) spectrum, q-major, y-shifted q order
+  float norm_h, norm_l;  // 1/sqrt(nx*ny) as hi/lo floats
+  double norm_d;
+};
+
+struct TemporalArgs {
+  const void* spec;
+  size_t Q;
+  int Tpad, T, nt, nlags;
+  FftPlan pt;
+  const void* twt;
+  const int* lags;       // device, nlags
+  const double* rcp;     // device, 1/(T - lag)
+  double* out;           // (nlags + 2, Q)
+  float invT_h, invT_l;
+  double invT_d;
+  float invnt_h, invnt_l;
+  double invnt_d;
+};
+
+enum Precision { PREC_FF = 0, PREC_F64 = 1, PREC_F32 = 2 };
+enum Mode { MODE_FFT = 0, MODE_DIFF = 1 };
+enum DType { DT_U8 = 0, DT_I16 = 1, DT_U16 = 2, DT_I32 = 3, DT_U32 = 4, DT_I64 = 5, DT_U64 = 6, DT_F32 = 7, DT_F64 = 8 };
+
+struct DdmRequest {
+  int mode;
+  int precision;
+  const void* img;
+  int dtype;
+  int64_t T, H, W;
+  std::vector<int> lags;
+  int64_t nx, ny, nt;
+  const double* window;  // device (H, W) or null
+  double* out;           // device (nlags + 2, ny, nx/2 + 1)
+  void* work;
+  size_t work_bytes;
+};
+
+struct WorkLayout {
+  size_t spec_off, spec_bytes;
+  size_t rbuf_off, rbuf_bytes;
+  size_t win_off, win_bytes;
+  size_t lags_off, rcp_off;
+  size_t total;
+  int Tpad, Hpad, chunk, pairs_per_block, cols_per_block, frames_per_block;
+};
+
+// Thread-local error message reported by fddm_b200_last_error().
+void set_last_error(const std::string& msg);
+int fail_with(int code, const std::string& msg);
+
+// Element size of the spectrum for a precision tier.
+size_t spec_elem_bytes(int precision);
+// Plan the workspace; returns false with a message when the problem is unsupported.
+bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err);
+// Factor n into supported radices; false if n has another prime factor.
+bool make_plan(int n, FftPlan& p);
+
+// Per-precision pipeline entry points (instantiated in ddm_ff.cu, ddm_f64.cu, ddm_f32.cu).
+int run_ddm_ff(const DdmRequest& r, cudaStream_t st, std::string& err);
+int run_ddm_f64(const DdmRequest& r, cudaStream_t st, std::string& err);
+int run_ddm_f32(const DdmRequest& r, cudaStream_t st, std::string& err);
+
+// Cached per-device FFT tables (twiddles in the requested scalar format, permutation).
+struct FftTables {
+  FftPlan plan;
+  const void* tw;
+  const int* perm;
+};
+// kind: 0 = ff (16 B twiddles), 1 = double, 2 = float
+bool get_tables(int n, int kind, FftTables& out, std::string& err);
+
+}  // namespace fddm

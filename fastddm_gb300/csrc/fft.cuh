@@ -1,0 +1,206 @@
+// In-place mixed-radix FFTs in shared memory, cooperatively executed by a CTA.
+//
+// Forward transforms are decimation-in-frequency (DIF) passes done in place:
+// pass s splits every block of M_s points into R_s interleaved sub-blocks,
+//     y_m = sum_r x[j + r*M_s/R_s] w_R^(r m),   then  y_m *= w_{M_s}^(j m),
+// and writes y_m back to x[j + m*M_s/R_s].  After all passes the spectrum sits
+// in mixed-radix digit-reversed order: X[k] is at position perm(k) with
+//     perm(k) = sum_s m_s * M_{s+1},   m_s = (k / (R_0...R_{s-1})) mod R_s.
+// The inverse transform runs the exact inverse of every pass in reverse order
+// (conjugate twiddle first, then the conjugate DFT), so it consumes the
+// permuted order and returns natural order.  A forward FFT, a pointwise
+// operation and an inverse FFT (the autocorrelation) therefore never reorders
+// data.  Because every butterfly reads and writes the same R locations, a
+// thread may process any number of butterflies per pass with R points in
+// registers; only a barrier separates passes.
+//
+// Radices: 2, 3, 4, 5, 7, 8, 11, 13 (covers every 2^a 3^b 5^c 7^d {1,11,13}
+// length).  Twiddles w_N^k = exp(-2 pi i k / N) come from a per-length table in
+// global memory computed on the host in extended precision.
+#pragma once
+#include "scalar.cuh"
+#include "dft_consts.cuh"
+#include "fddm_internal.h"
+
+namespace fddm {
+
+template <class S, int R> struct odd_off;
+template <class S> struct odd_off<S, 3> { static constexpr int v = 0; };
+template <class S> struct odd_off<S, 5> { static constexpr int v = 3; };
+template <class S> struct odd_off<S, 7> { static constexpr int v = 8; };
+template <class S> struct odd_off<S, 11> { static constexpr int v = 15; };
+template <class S> struct odd_off<S, 13> { static constexpr int v = 26; };
+
+template <class S> __device__ __forceinline__ S kcos(int idx) {
+  return sc<S>::cst(kCosH[idx], kCosL[idx], kCosD[idx]);
+}
+template <class S> __device__ __forceinline__ S ksin(int idx) {
+  return sc<S>::cst(kSinH[idx], kSinL[idx], kSinD[idx]);
+}
+
+// ---------------------------------------------------------------------------
+// In-register DFTs of size R (forward: w = exp(-2 pi i / R); INV: conjugate).
+// ---------------------------------------------------------------------------
+template <class S, bool INV> __device__ __forceinline__ void dft2(cx<S>* v) {
+  cx<S> a = cadd(v[0], v[1]);
+  cx<S> b = csub(v[0], v[1]);
+  v[0] = a;
+  v[1] = b;
+}
+
+template <class S, bool INV>
+__device__ __forceinline__ void dft4_vals(cx<S>& x0, cx<S>& x1, cx<S>& x2, cx<S>& x3) {
+  cx<S> t0 = cadd(x0, x2);
+  cx<S> t1 = csub(x0, x2);
+  cx<S> t2 = cadd(x1, x3);
+  cx<S> t3 = cmul_mi<S, INV>(csub(x1, x3));
+  x0 = cadd(t0, t2);
+  x2 = csub(t0, t2);
+  x1 = cadd(t1, t3);
+  x3 = csub(t1, t3);
+}
+
+template <class S, bool INV> __device__ __forceinline__ void dft4(cx<S>* v) {
+  dft4_vals<S, INV>(v[0], v[1], v[2], v[3]);
+}
+
+template <class S, bool INV> __device__ __forceinline__ void dft8(cx<S>* v) {
+  const S h = sc<S>::cst(kSqrtHalfH, kSqrtHalfL, kSqrtHalfD);
+  cx<S> a0 = cadd(v[0], v[4]), a1 = cadd(v[1], v[5]), a2 = cadd(v[2], v[6]), a3 = cadd(v[3], v[7]);
+  cx<S> b0 = csub(v[0], v[4]), b1 = csub(v[1], v[5]), b2 = csub(v[2], v[6]), b3 = csub(v[3], v[7]);
+  // b_r *= w8^r  (forward w8 = (1 - i)/sqrt2, inverse its conjugate)
+  if (!INV) {
+    b1 = cscale<S>({sc<S>::add(b1.r, b1.i), sc<S>::sub(b1.i, b1.r)}, h);
+    b3 = cscale<S>({sc<S>::sub(b3.i, b3.r), sc<S>::neg(sc<S>::add(b3.r, b3.i))}, h);
+  } else {
+    b1 = cscale<S>({sc<S>::sub(b1.r, b1.i), sc<S>::add(b1.r, b1.i)}, h);
+    b3 = cscale<S>({sc<S>::neg(sc<S>::add(b3.r, b3.i)), sc<S>::sub(b3.r, b3.i)}, h);
+  }
+  b2 = cmul_mi<S, INV>(b2);
+  dft4_vals<S, INV>(a0, a1, a2, a3);
+  dft4_vals<S, INV>(b0, b1, b2, b3);
+  v[0] = a0; v[2] = a1; v[4] = a2; v[6] = a3;
+  v[1] = b0; v[3] = b1; v[5] = b2; v[7] = b3;
+}
+
+// Odd radix via conjugate-pair symmetry: R^2/4 complex-by-real products.
+template <class S, int R, bool INV> __device__ __forceinline__ void dft_odd(cx<S>* v) {
+  constexpr int H = (R - 1) / 2;
+  constexpr int OFF = odd_off<S, R>::v;
+  cx<S> a[H], b[H];
+#pragma unroll
+  for (int r = 1; r <= H; ++r) {
+    a[r - 1] = cadd(v[r], v[R - r]);
+    b[r - 1] = csub(v[r], v[R - r]);
+  }
+  cx<S> x0 = v[0];
+  cx<S> y0 = x0;
+#pragma unroll
+  for (int r = 0; r < H; ++r) y0 = cadd(y0, a[r]);
+#pragma unroll
+  for (int m = 1; m <= H; ++m) {
+    cx<S> re = x0;
+    cx<S> im = czero<S>();
+#pragma unroll
+    for (int r = 1; r <= H; ++r) {
+      const int idx = OFF + (r * m) % R;
+      const S c = kcos<S>(idx);
+      const S s = ksin<S>(idx);
+      re = cadd(re, cscale(a[r - 1], c));
+      im = cadd(im, cscale(b[r - 1], s));
+    }
+    // forward: y_m = re - i*im, y_{R-m} = re + i*im
+    cx<S> mi = cmul_mi<S, false>(im);  // -i * im
+    if (!INV) {
+      v[m] = cadd(re, mi);
+      v[R - m] = csub(re, mi);
+    } else {
+      v[m] = csub(re, mi);
+      v[R - m] = cadd(re, mi);
+    }
+  }
+  v[0] = y0;
+}
+
+template <class S, int R, bool INV> __device__ __forceinline__ void dft(cx<S>* v) {
+  if constexpr (R == 2) dft2<S, INV>(v);
+  else if constexpr (R == 4) dft4<S, INV>(v);
+  else if constexpr (R == 8) dft8<S, INV>(v);
+  else dft_odd<S, R, INV>(v);
+}
+
+// ---------------------------------------------------------------------------
+// One in-place pass over `nfft` transforms of length n, stored at buf + f*ld.
+// ---------------------------------------------------------------------------
+template <class S, int R, bool INV>
+__device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int ld, int n, int M,
+                                         const cx<S>* __restrict__ tw, int tid, int nthr) {
+  const int stride = M / R;
+  const int bpf = n / R;
+  const int twstep = n / M;
+  const int total = nfft * bpf;
+  for (int beta = tid; beta < total; beta += nthr) {
+    const int f = beta / bpf;
+    const int loc = beta - f * bpf;
+    const int blk = loc / stride;
+    const int j = loc - blk * stride;
+    cx<S>* p = buf + (size_t)f * ld + blk * M + j;
+    cx<S> v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = p[r * stride];
+    if (!INV) {
+      dft<S, R, false>(v);
+      if (j != 0) {
+#pragma unroll
+        for (int m = 1; m < R; ++m) v[m] = cmul(v[m], tw[twstep * j * m]);
+      }
+    } else {
+      if (j != 0) {
+#pragma unroll
+        for (int m = 1; m < R; ++m) v[m] = cmulc(v[m], tw[twstep * j * m]);
+      }
+      dft<S, R, true>(v);
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) p[r * stride] = v[r];
+  }
+}
+
+template <class S, bool INV>
+__device__ __forceinline__ void fft_pass_dispatch(cx<S>* buf, int nfft, int ld, int n, int M, int R,
+                                                  const cx<S>* tw, int tid, int nthr) {
+  switch (R) {
+    case 2: fft_pass<S, 2, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
+    case 3: fft_pass<S, 3, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
+    case 4: fft_pass<S, 4, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
+    case 5: fft_pass<S, 5, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
+    case 7: fft_pass<S, 7, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
+    case 8: fft_pass<S, 8, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
+    case 11: fft_pass<S, 11, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
+    case 13: fft_pass<S, 13, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
+    default: break;
+  }
+}
+
+// Forward DIF: natural order in, digit-reversed (perm) order out.
+// Caller synchronises before the call; the function ends with a barrier.
+template <class S>
+__device__ void fft_forward(cx<S>* buf, int nfft, int ld, const FftPlan& p, const cx<S>* tw, int tid,
+                            int nthr) {
+  for (int s = 0; s < p.npass; ++s) {
+    fft_pass_dispatch<S, false>(buf, nfft, ld, p.n, p.block[s], p.radix[s], tw, tid, nthr);
+    __syncthreads();
+  }
+}
+
+// Inverse (unnormalised, sum_k X_k w^(-jk)): perm order in, natural order out.
+template <class S>
+__device__ void fft_inverse(cx<S>* buf, int nfft, int ld, const FftPlan& p, const cx<S>* tw, int tid,
+                            int nthr) {
+  for (int s = p.npass - 1; s >= 0; --s) {
+    fft_pass_dispatch<S, true>(buf, nfft, ld, p.n, p.block[s], p.radix[s], tw, tid, nthr);
+    __syncthreads();
+  }
+}
+
+}  // namespace fddm

@@ -1,0 +1,129 @@
+/*
+ * fddm_b200.h - C ABI of the GB300 (sm_103a) image-structure-function core.
+ *
+ * This library is the device-side replacement of FastDDM's native cores for the
+ * path  fastddm.ddm(img_seq, lags, mode='fft'|'diff', window=...)  and of the
+ * binning loops of fastddm.azimuthal_average.  Every function:
+ *   - returns an int status (FDDM_OK == 0) and never exits or aborts the process;
+ *     the message of the last failure on the calling thread is available from
+ *     fddm_b200_last_error();
+ *   - takes caller-owned DEVICE buffers (plain pointers and sizes) and a CUDA
+ *     stream passed as void* (a cudaStream_t; NULL = legacy default stream);
+ *   - enqueues work on that stream and returns without synchronising.
+ * The library keeps one cache per device: FFT twiddle and permutation tables,
+ * allocated on first use of a transform length.
+ *
+ * Reference interfaces replaced (paths inside the FastDDM source tree):
+ *   src/cpp/ddm.h:54-61        ddm_fft<T>(img_seq, lags, nx, ny, nt, chunk_size, window)
+ *   src/cpp/ddm.h:38-43        ddm_diff<T>(img_seq, lags, nx, ny, window)
+ *   src/cuda/ddm_cuda.h:53     ddm_fft_cuda<T>(...)   (same contract, cuFFT/FP64)
+ *   src/cuda/ddm_cuda.h:38     ddm_diff_cuda<T>(...)
+ *   src/python/bindings/ddm_bindings.h:25-43   one overload per input dtype
+ *   src/python/azimuthalaverage.py:277-478     azimuthal_average_array binning
+ */
+#ifndef FDDM_B200_H
+#define FDDM_B200_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FDDM_OK 0
+#define FDDM_ERR_INVALID 1     /* bad argument (sizes, lags, dtype, null pointer) */
+#define FDDM_ERR_NOMEM 2       /* workspace too small / device allocation failed */
+#define FDDM_ERR_CUDA 3        /* a CUDA runtime call or kernel launch failed */
+#define FDDM_ERR_UNSUPPORTED 4 /* valid input this build cannot process (e.g. T too long) */
+
+/* input pixel types: the nine dtypes the reference binds (ddm_bindings.h:25-43).
+   64-bit integers are converted to double by the caller, as the reference's
+   cast to Scalar does (ddm.cc:288-297); the kernels accept the other seven. */
+#define FDDM_U8 0
+#define FDDM_I16 1
+#define FDDM_U16 2
+#define FDDM_I32 3
+#define FDDM_U32 4
+#define FDDM_I64 5
+#define FDDM_U64 6
+#define FDDM_F32 7
+#define FDDM_F64 8
+
+/* arithmetic tiers */
+#define FDDM_PREC_FF 0  /* float-float (~48-bit) FFTs and sums on FP32 pipes: FP64-class accuracy */
+#define FDDM_PREC_F64 1 /* native FP64 everywhere (the reference's arithmetic, slow on GB300) */
+#define FDDM_PREC_F32 2 /* FP32 FFTs, float-float sums and combination (fast, ~1e-4 relative) */
+
+/* modes */
+#define FDDM_MODE_FFT 0  /* Wiener-Khinchin: autocorrelation by zero-padded temporal FFT */
+#define FDDM_MODE_DIFF 1 /* direct differences <|F(t+lag) - F(t)|^2>_t */
+
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+int fddm_b200_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* fddm_b200_last_error(void);
+
+/* Device workspace (bytes) needed by fddm_b200_ddm_fft / _diff for these sizes.
+   Replaces the host/device memory planners of the reference
+   (src/python/_ddm_cpp.py:114-139, src/cuda/memchk_gpu.cu:653-702).
+   nt is ignored for FDDM_MODE_DIFF. */
+int fddm_b200_workspace_size(int mode, int precision, uint64_t length, uint64_t height, uint64_t width,
+                             uint64_t nlags, uint64_t nx, uint64_t ny, uint64_t nt, int has_window,
+                             size_t* bytes);
+
+/* Image structure function, fft mode.  Replaces ddm_fft<T> (src/cpp/ddm.h:54-61,
+   src/cpp/ddm.cc:250-453) and ddm_fft_cuda<T> (src/cuda/ddm_cuda.h:53).
+     d_img_seq   (length, height, width) C-contiguous frames of `dtype`
+     lags        HOST array of nlags lags in [0, length-1] (the reference's vector<unsigned>)
+     nx, ny      padded FFT sizes (>= width, height; factors 2,3,5,7,11,13)
+     nt          temporal FFT length, >= 2*length-1 (factors 2,3,5,7,11,13)
+     d_window    (height, width) FP64 window or NULL (the reference's empty window)
+     d_out       (nlags + 2, ny, nx/2 + 1) FP64 output: D(lag) rows in the order of
+                 `lags`, then the power spectrum, then the variance; rows y-fftshifted
+                 exactly as make_shifted_isf (src/cpp/helper_ddm.cc:41-103) leaves them.
+     d_workspace at least fddm_b200_workspace_size(...) bytes.
+   chunk_size of the reference has no counterpart: the q axis is never chunked. */
+int fddm_b200_ddm_fft(const void* d_img_seq, int dtype, uint64_t length, uint64_t height, uint64_t width,
+                      const uint32_t* lags, uint64_t nlags, uint64_t nx, uint64_t ny, uint64_t nt,
+                      const double* d_window, double* d_out, void* d_workspace, size_t workspace_bytes,
+                      int precision, void* stream);
+
+/* Image structure function, diff mode.  Replaces ddm_diff<T> (src/cpp/ddm.h:38-43,
+   src/cpp/ddm.cc:37-192) and ddm_diff_cuda<T> (src/cuda/ddm_cuda.h:38).
+   Arguments as fddm_b200_ddm_fft without nt. */
+int fddm_b200_ddm_diff(const void* d_img_seq, int dtype, uint64_t length, uint64_t height, uint64_t width,
+                       const uint32_t* lags, uint64_t nlags, uint64_t nx, uint64_t ny,
+                       const double* d_window, double* d_out, void* d_workspace, size_t workspace_bytes,
+                       int precision, void* stream);
+
+/* Weighted azimuthal average of a stack of half-plane maps: the per-(bin, row)
+   weighted mean and unbiased weighted standard deviation.  Replaces the two
+   per-pixel loops of azimuthal_average_array (src/python/azimuthalaverage.py:435-444
+   and :457-476) as called by azimuthal_average (:481-564).  The caller does the
+   O(pixels) set-up the reference does before those loops (bin search, masking,
+   sum of weights per bin, :394-432) and passes each bin's pixels in increasing
+   pixel order.  One thread accumulates one (bin, row) in that order with the
+   reference's operation order and IEEE round-to-nearest FP64 operations, so the
+   result does not depend on scheduling.
+     d_data        (nrows, npix) FP64 maps (the structure function's _data)
+     d_bin_offsets nbins + 1 offsets into d_bin_pixels (CSR)
+     d_bin_pixels  pixel indices of every bin, increasing within a bin
+     d_weight      npix FP64 weight per pixel (counts x weights)
+     d_sumw        nbins FP64 sum of weights per bin
+     d_bias        nbins FP64 sum_w - sum_w2/sum_w (or NULL when d_err is NULL)
+     d_avg         (nbins, nrows) out: weighted mean; NaN where sum_w == 0
+     d_err         (nbins, nrows) out: sqrt(sum w (x - mean)^2 / bias); NaN where
+                   sum_w == 0; NULL to skip */
+int fddm_b200_azimuthal_average(const double* d_data, uint64_t nrows, uint64_t npix,
+                                const int32_t* d_bin_offsets, const int32_t* d_bin_pixels, uint64_t nbins,
+                                const double* d_weight, const double* d_sumw, const double* d_bias,
+                                double* d_avg, double* d_err, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FDDM_B200_H */

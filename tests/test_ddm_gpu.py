@@ -1,0 +1,165 @@
+"""Parity of the GB300 structure-function kernels with the FP64 oracle (needs a GPU).
+
+Tolerances (max elementwise relative error of every output row, the DC mode
+included) against the FP64 restatement of the reference's ``cpp`` core:
+  ff  (float-float FFTs and sums)        <= 1e-9
+  f64 (native FP64)                      <= 1e-10
+  f32 (FP32 FFTs, float-float sums)      <= 5e-2 (reported only; FP32 FFTs cannot reach 1e-6)
+The reference's own cross-core tests accept np.isclose (rtol 1e-5, atol 1e-8).
+"""
+
+import numpy as np
+import pytest
+
+import ddm_oracle as oracle
+from conftest import gpu_ready
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_ready(), reason="needs a CUDA GPU")]
+
+TOL = {"ff": 1e-9, "f64": 1e-10, "f32": 5e-2}
+
+
+@pytest.fixture(scope="module")
+def fddm(built_lib):
+    import fastddm_gb300
+
+    return fastddm_gb300
+
+
+def _oracle(imgs, lags, mode, window=None):
+    T, H, W = imgs.shape
+    nx, ny = oracle.next_fast_len_cpp(W), oracle.next_fast_len_cpp(H)
+    lags = oracle.prepare_lags(lags, T)
+    if mode == "fft":
+        return oracle.ddm_fft(imgs, lags, nx, ny, oracle.next_fast_len_cpp(2 * T), window)
+    return oracle.ddm_diff(imgs, lags, nx, ny, window)
+
+
+def _poisson_stack(shape, dtype, seed=0, level=300.0):
+    rng = np.random.default_rng(seed)
+    T, H, W = shape
+    yy, xx = np.mgrid[0:H, 0:W]
+    frames = []
+    for t in range(T):
+        cx, cy = (0.3 + 0.01 * t) * W, (0.6 - 0.01 * t) * H
+        scene = level + 8 * level * np.exp(-((xx - cx) ** 2 + (yy - cy) ** 2) / (0.02 * H * W + 2))
+        frames.append(rng.poisson(scene))
+    a = np.stack(frames)
+    if np.dtype(dtype).kind in "ui":
+        info = np.iinfo(dtype)
+        a = np.clip(a, info.min, info.max)
+    return a.astype(dtype)
+
+
+@pytest.mark.parametrize("precision", ["ff", "f64", "f32"])
+@pytest.mark.parametrize("mode", ["fft", "diff"])
+@pytest.mark.parametrize("case,winkey,outkey", [
+    ("A", None, "A_{mode}"),
+    ("A", "A_window", "A_{mode}_win"),
+    ("B", "B_window", "B_{mode}"),
+])
+def test_golden_vectors(fddm, golden, precision, mode, case, winkey, outkey):
+    """The reference's own test fixture (confocal frames, lags 1..9) and a padded odd-size case."""
+    imgs, lags = golden[f"{case}_imgs"], golden[f"{case}_lags"]
+    w = golden[winkey] if winkey else None
+    r = fddm.ddm(imgs, lags, mode=mode, window=w, precision=precision)
+    ref = golden[outkey.format(mode=mode)]
+    assert r._data.shape == ref.shape
+    np.testing.assert_array_equal(r.kx, golden[f"{case}_kx"])
+    np.testing.assert_array_equal(r.ky, golden[f"{case}_ky"])
+    err = oracle.rel_err(r._data, ref)
+    print(f"{case} {mode} {precision} window={winkey is not None}: max rel err {err:.3e}")
+    assert err < max(TOL[precision], 2e-11)
+    if precision != "f32":
+        assert np.isclose(r._data, ref).all()
+
+
+@pytest.mark.parametrize("precision", ["ff", "f64"])
+@pytest.mark.parametrize("mode", ["fft", "diff"])
+@pytest.mark.parametrize("dtype", ["uint8", "int16", "uint16", "int32", "uint32", "float32", "float64", "int64"])
+def test_dtypes(fddm, precision, mode, dtype):
+    imgs = _poisson_stack((10, 16, 24), dtype, seed=3, level=20.0 if dtype == "uint8" else 300.0)
+    lags = [1, 2, 4, 9]
+    r = fddm.ddm(imgs, lags, mode=mode, precision=precision)
+    ref = _oracle(imgs, lags, mode)
+    assert oracle.rel_err(r._data, ref) < TOL[precision]
+
+
+@pytest.mark.parametrize("shape", [
+    (7, 13, 11),     # radices 13 and 11, nt = 14 (2 x 7)
+    (9, 25, 49),     # 5 x 5 and 7 x 7
+    (33, 30, 45),    # odd width -> nx = 45, nt = 66
+    (16, 19, 23),    # padded: 19 -> 20, 23 -> 24
+    (40, 64, 96),    # 96 = 2^5 x 3
+    (3, 2, 2),       # tiny frames
+])
+@pytest.mark.parametrize("mode", ["fft", "diff"])
+def test_shapes_and_radices(fddm, shape, mode):
+    imgs = _poisson_stack(shape, "uint16", seed=sum(shape))
+    T = shape[0]
+    lags = sorted({1, 2, T // 2, T - 1})
+    w = fddm.window.blackman_harris(shape)
+    for window in (None, w):
+        r = fddm.ddm(imgs, lags, mode=mode, window=window, precision="ff")
+        ref = _oracle(imgs, lags, mode, window)
+        err = oracle.rel_err(r._data, ref)
+        assert err < TOL["ff"], (shape, mode, window is not None, err)
+
+
+def test_config1_all_lags_fft_vs_oracle_and_diff(fddm):
+    """64 frames of 128 x 128 uint16 Brownian spots, lags 1..63, no window."""
+    from fastddm_gb300.synthetic import CONFIG1, make_stack
+
+    imgs = make_stack(CONFIG1)
+    lags = np.arange(1, 64)
+    fft = fddm.ddm(imgs, lags, mode="fft")._data
+    diff = fddm.ddm(imgs, lags, mode="diff")._data
+    ref_fft = _oracle(imgs, lags, "fft")
+    ref_diff = _oracle(imgs, lags, "diff")
+    e = {
+        "fft_vs_cpp_fft": oracle.rel_err(fft, ref_fft),
+        "fft_vs_cpp_diff": oracle.rel_err(fft, ref_diff),
+        "fft_vs_cpp_diff_noDC": oracle.rel_err(fft, ref_diff, skip_dc=True),
+        "diff_vs_cpp_diff": oracle.rel_err(diff, ref_diff),
+        "fft_vs_diff": oracle.rel_err(fft, diff),
+    }
+    print(e)
+    assert all(v < 1e-6 for v in e.values()), e
+
+
+def test_edge_cases(fddm):
+    imgs = _poisson_stack((6, 8, 10), "uint16")
+    # only lag 0 -> removed, output holds PS and VAR only
+    with pytest.warns(UserWarning):
+        r = fddm.ddm(imgs, [0], mode="fft")
+    assert r._data.shape == (2, 8, 6)
+    ref = _oracle(imgs, [0], "fft")
+    assert oracle.rel_err(r._data, ref) < TOL["ff"]
+    # a single frame: no lags at all
+    one = imgs[:1]
+    with pytest.warns(UserWarning):
+        r1 = fddm.ddm(one, [0], mode="diff")
+    np.testing.assert_allclose(r1.var, 0.0, atol=1e-9 * np.max(r1.power_spec))
+    # duplicated / unsorted lags are deduplicated and sorted
+    r2 = fddm.ddm(imgs, [5, 1, 3, 1], mode="fft")
+    np.testing.assert_array_equal(r2.tau, [1.0, 3.0, 5.0])
+    ref2 = _oracle(imgs, [1, 3, 5], "fft")
+    assert oracle.rel_err(r2._data, ref2) < TOL["ff"]
+
+
+def test_repeat_calls_identical(fddm):
+    """Same input, same plan: bitwise identical results (no atomics in the pipeline)."""
+    imgs = _poisson_stack((20, 32, 32), "uint16", seed=7)
+    a = fddm.ddm(imgs, range(1, 20), mode="fft")._data
+    b = fddm.ddm(imgs, range(1, 20), mode="fft")._data
+    np.testing.assert_array_equal(a, b)
+
+
+def test_backend_function_contract(fddm):
+    """The registry functions take the reference's positional arguments and return the raw array."""
+    imgs = _poisson_stack((8, 12, 16), "uint8", level=30.0)
+    lags = np.array([1, 3])
+    out = fddm._backend["b200"]["fft"](imgs, lags, 16, 12, 16, np.array([], dtype=np.float64))
+    assert out.dtype == np.float64 and out.shape == (4, 12, 9)
+    out2 = fddm._backend["b200"]["diff"](imgs, lags, 16, 12, np.array([], dtype=np.float64), gpu_id=0)
+    assert oracle.rel_err(out, out2) < 1e-9
