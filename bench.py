@@ -1,0 +1,396 @@
+"""Benchmark: DDM frames/s of the b200 core on one GB300 (replicas on N GPUs).
+
+Workload (default ``--config large``): one stack of 4000 frames of 1024 x 1024
+uint8 (seeded Brownian-spot scene with drift and Poisson noise), 200
+log-spaced lags 1..3999, fft mode, float-float tier.  A step is one full
+structure-function computation of the stack (spatial FFTs, temporal
+autocorrelation, combination); the stack (4.2 GB) and the spectrum (34 GB) are
+far larger than L2, so no flush is needed between steps.
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the CPU restatement
+of the reference's FP64 core on the host cores instead.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+CONFIGS = {
+    # name: (scene attribute, lags builder, mode)
+    "large": "CONFIG3",
+    "medium": "CONFIG2",
+    "small": "CONFIG1",
+}
+
+
+def lags_for(name: str, T: int) -> np.ndarray:
+    from fastddm_gb300 import lags as lg
+
+    if name == "large":
+        return np.unique(lg.logspace_int(T - 1, num=200, endpoint=True))
+    return np.arange(1, T)
+
+
+def workload_desc(name, scene, lags, precision, mode):
+    return {
+        "workload": f"ddm_{mode}_{scene.length}x{scene.height}x{scene.width}_{scene.dtype}_{len(lags)}lags",
+        "frames": scene.length, "height": scene.height, "width": scene.width, "pixel_dtype": scene.dtype,
+        "lags": int(len(lags)), "mode": mode, "precision": precision,
+        "window": "blackman_harris" if name == "medium" else None,
+        "scene": {"spots": scene.n_spots, "sigma": scene.sigma, "amplitude": scene.amplitude,
+                  "diffusivity": scene.diffusivity, "offset": scene.offset, "drift": scene.drift,
+                  "seed": scene.seed},
+        "l2_flush": "inputs larger than L2 (stack and spectrum > 129 MB)",
+        "parallelism": "replicas",
+    }
+
+
+# ---------------------------------------------------------------------------
+# CPU sample work (the oracle port); module-level so a spawn pool can run it
+# ---------------------------------------------------------------------------
+def _cpu_spatial(args):
+    frames, nx, ny = args
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import ddm_oracle as oracle
+
+    t0 = time.perf_counter()
+    oracle.spatial_fft(frames, nx, ny, None)
+    return time.perf_counter() - t0, frames.shape[0]
+
+
+def _cpu_temporal(args):
+    T, nq, lags, nt, seed = args
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import ddm_oracle as oracle
+
+    rng = np.random.default_rng(seed)
+    Fq = rng.standard_normal((T, nq)) + 1j * rng.standard_normal((T, nq))
+    t0 = time.perf_counter()
+    oracle.temporal_fft(Fq, lags, nt)
+    return time.perf_counter() - t0, nq
+
+
+def cpu_throughput(frames_sample: np.ndarray, T: int, Q: int, nx: int, ny: int, nt: int, lags, workers: int,
+                   spatial_frames: int, temporal_q: int, pool=None):
+    """Frames/s of the full job estimated from timed samples of both stages.
+
+    Spatial stage: `spatial_frames` frames per worker; temporal stage:
+    `temporal_q` spectrum columns of length T per worker.  Job time =
+    T / spatial rate + Q / temporal rate; frames/s = T / job time.
+    """
+    sp_args = [(frames_sample[:spatial_frames], nx, ny) for _ in range(workers)]
+    tq_args = [(T, temporal_q, list(lags), nt, i) for i in range(workers)]
+    if pool is None:
+        sp = [_cpu_spatial(a) for a in sp_args]
+        t0 = time.perf_counter()
+        sp = [_cpu_spatial(a) for a in sp_args]
+        sp_wall = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        tq = [_cpu_temporal(a) for a in tq_args]
+        tq_wall = time.perf_counter() - t0
+    else:
+        t0 = time.perf_counter()
+        sp = list(pool.map(_cpu_spatial, sp_args))
+        sp_wall = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        tq = list(pool.map(_cpu_temporal, tq_args))
+        tq_wall = time.perf_counter() - t0
+    sp_rate = sum(n for _, n in sp) / sp_wall  # frames / s
+    tq_rate = sum(n for _, n in tq) / tq_wall  # q columns / s
+    job = T / sp_rate + Q / tq_rate
+    return T / job, sp_wall + tq_wall
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        pw = [num(r[3]) for r in rows if num(r[3]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(pw) if pw else None, "samples": len(rows), "reasons": reasons}
+
+
+# ---------------------------------------------------------------------------
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    from concurrent.futures import ProcessPoolExecutor
+    import multiprocessing as mp
+
+    from fastddm_gb300 import synthetic
+    from fastddm_gb300._fftopt import next_fast_len
+
+    scene = getattr(synthetic, CONFIGS[args.config])
+    lags = lags_for(args.config, scene.length)
+    T, H, W = scene.length, scene.height, scene.width
+    nx, ny, nt = next_fast_len(W, "cpp"), next_fast_len(H, "cpp"), next_fast_len(2 * T, "cpp")
+    Q = ny * (nx // 2 + 1)
+    small = synthetic.Scene(4, H, W, max(1, scene.n_spots), scene.sigma, scene.amplitude, scene.diffusivity,
+                            scene.offset, scene.drift, scene.dtype, scene.seed)
+    frames = synthetic.make_stack(small)
+    workers = os.cpu_count() or 1
+    values = []
+    with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as pool:
+        for i in range(args.warmup + args.steps):
+            v, _ = cpu_throughput(frames, T, Q, nx, ny, nt, lags, workers, 2, 64, pool)
+            if i >= args.warmup:
+                values.append(v)
+    value = statistics.mean(values)
+    line = {
+        "impl": "reference", "metric": "DDM frames/s", "value": value, "unit": "frames/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * T / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_desc(args.config, scene, lags, "f64", "fft"),
+        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": workers, "kind": "port",
+                         "sample": f"per step and worker: spatial FFT of 2 frames and the temporal stage of 64 "
+                                   f"q-columns x {T} frames; full-job time extrapolated as T/spatial_rate + "
+                                   f"Q/temporal_rate (numpy FP64 restatement of the cpp core; the cpp core itself "
+                                   f"needs FFTW's CMake build)"},
+        "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+
+    ws, rank, local = dist_setup()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+
+    from fastddm_gb300 import _build, _lib, synthetic, window as fwin
+    from fastddm_gb300._ddm_b200 import DdmPlan, ddm_fft_b200
+    from fastddm_gb300._fftopt import next_fast_len
+
+    _build.build()
+    lib = _lib.load()
+    scene = getattr(synthetic, CONFIGS[args.config])
+    lags = lags_for(args.config, scene.length)
+    T, H, W = scene.length, scene.height, scene.width
+    nx, ny = next_fast_len(W, "b200"), next_fast_len(H, "b200")
+    nt = next_fast_len(2 * T, "b200")
+    nkx = nx // 2 + 1
+    Q = ny * nkx
+    L = len(lags)
+    frames = synthetic.make_stack_torch(scene, device=device)
+    code = {torch.uint8: 0, torch.int16: 1}.get(frames.dtype, 2)
+    window = None
+    if args.config == "medium":
+        window = torch.from_numpy(fwin.blackman_harris((H, W))).to(device)
+    plan = DdmPlan(args.mode, T, H, W, code, lags, nx, ny, nt if args.mode == "fft" else 0, window is not None,
+                   args.precision, device)
+    out = torch.empty(plan.out_shape, dtype=torch.float64, device=device)
+    stream = torch.cuda.current_stream(device)
+    for _ in range(args.warmup):
+        plan.run(frames, window, out, stream)
+    torch.cuda.synchronize(device)
+
+    launches0 = lib.fddm_b200_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(device)
+        e0.record(stream)
+        for _ in range(args.steps):
+            plan.run(frames, window, out, stream)
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        if ws > 1:
+            torch.distributed.barrier()
+    launches = int(lib.fddm_b200_launch_count() - launches0)
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([ms], device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = ws * T * args.steps / (ms / 1000.0)
+    clocks = clk.summary()
+
+    # per-stage device times (untimed extra steps with CUDA events around each stage)
+    import ctypes
+
+    lib.fddm_b200_set_stage_timing(1)
+    sp, tp = [], []
+    for _ in range(2):
+        plan.run(frames, window, out, stream)
+        a, b = ctypes.c_float(), ctypes.c_float()
+        _lib.check(lib.fddm_b200_stage_times(ctypes.byref(a), ctypes.byref(b)))
+        sp.append(a.value)
+        tp.append(b.value)
+    lib.fddm_b200_set_stage_timing(0)
+    sp_ms, tp_ms = statistics.mean(sp), statistics.mean(tp)
+
+    es = 16 if args.precision in ("ff", "f64") else 8
+    b_in = frames.element_size()
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        peak_src = "measured"
+    except (OSError, ValueError):
+        peak_src = "fallback"
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    # algorithmic bytes per launch of the temporal kernel: read the spectrum once, write the output
+    tfft_bytes = T * Q * es + (L + 2) * Q * 8
+    # spatial stage (row + column passes): read frames, write the spectrum once
+    spatial_bytes = T * H * W * b_in + T * Q * es
+    job_bytes = T * H * W * b_in + 2 * T * Q * es + (L + 2) * Q * 8
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get(f"{args.config}:{args.mode}:{args.precision}")
+        except ValueError:
+            traffic = None
+    dominant = "k_tfft" if tp_ms >= sp_ms else "k_rows+k_cols"
+    if dominant == "k_tfft":
+        ach = tfft_bytes / (tp_ms / 1000.0) / 1e9
+        tr = traffic.get("k_tfft") if isinstance(traffic, dict) else None
+    else:
+        ach = spatial_bytes / (sp_ms / 1000.0) / 1e9
+        tr = traffic.get("spatial") if isinstance(traffic, dict) else None
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": ach, "peak": hbm, "unit": "GB/s",
+                "frac": ach / hbm, "traffic": tr, "peak_source": peak_src,
+                "stage_ms": {"spatial": sp_ms, "temporal": tp_ms},
+                "job_bytes": job_bytes, "job_frac": job_bytes / (ms_step / 1000.0) / 1e9 / hbm}
+
+    # end to end through the public API: pinned host frames in, host result out
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        host = torch.empty(frames.shape, dtype=frames.dtype, pin_memory=True)
+        host.copy_(frames)
+        del plan, out
+        torch.cuda.empty_cache()
+        wnp = window.cpu().numpy() if window is not None else np.array([], dtype=np.float64)
+        fn = ddm_fft_b200
+        res = fn(host, lags, nx, ny, nt, wnp, precision=args.precision)  # warm-up (allocations)
+        times = []
+        for _ in range(max(1, args.steps)):
+            torch.cuda.synchronize(device)
+            t0 = time.perf_counter()
+            res = fn(host, lags, nx, ny, nt, wnp, precision=args.precision)
+            times.append(time.perf_counter() - t0)
+        e2e = {"value": T / statistics.mean(times), "unit": "frames/s",
+               "h2d_bytes_per_step": int(host.numel() * host.element_size()),
+               "d2h_bytes_per_step": int(res.nbytes), "ms_per_step": 1000 * statistics.mean(times)}
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and ws == 1:
+        sample = frames[:2].cpu().numpy()
+        v, wall = cpu_throughput(sample, T, Q, nx, ny, nt, lags, 1, 2, 256, None)
+        cpu = {"value": v, "unit": "frames/s", "cores": 1, "kind": "port",
+               "sample": f"spatial FFT of 2 frames and the temporal stage of 256 q-columns x {T} frames "
+                         f"(FP64 numpy restatement of the cpp core), extrapolated to the full job; {wall:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": "DDM frames/s", "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": {"ff": "ff (float-float)", "f64": "f64", "f32": "f32"}[args.precision],
+            "data": "synthetic", "config": workload_desc(args.config, scene, lags, args.precision, args.mode),
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="large", choices=sorted(CONFIGS))
+    ap.add_argument("--mode", default="fft", choices=["fft", "diff"])
+    ap.add_argument("--precision", default="ff", choices=["ff", "f64", "f32"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

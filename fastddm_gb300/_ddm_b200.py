@@ -199,13 +199,20 @@ def ddm_device(img_seq, lags: Sequence[int], nx: int, ny: int, nt: int, window=N
     return out
 
 
+def to_host(out: "torch.Tensor") -> np.ndarray:
+    """Device result -> numpy array, through page-locked memory (the array keeps it alive)."""
+    host = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
+    host.copy_(out)
+    return host.numpy()
+
+
 def ddm_fft_b200(img_seq, lags, nx, ny, nt, window, *, gpu_id: int = 0, precision: str = "ff", **kwargs) -> np.ndarray:
     """Image structure function, fft mode (Wiener-Khinchin), on the GB300."""
     out = ddm_device(img_seq, lags, nx, ny, nt, window, mode="fft", precision=precision, gpu_id=gpu_id)
-    return out.cpu().numpy()
+    return to_host(out)
 
 
 def ddm_diff_b200(img_seq, lags, nx, ny, window, *, gpu_id: int = 0, precision: str = "ff", **kwargs) -> np.ndarray:
     """Image structure function, diff mode (direct differences), on the GB300."""
     out = ddm_device(img_seq, lags, nx, ny, 0, window, mode="diff", precision=precision, gpu_id=gpu_id)
-    return out.cpu().numpy()
+    return to_host(out)

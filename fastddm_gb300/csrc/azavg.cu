@@ -69,5 +69,6 @@ extern "C" int fddm_b200_azimuthal_average(const double* d_data, uint64_t nrows,
                                                               d_avg, d_err);
   const cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) return fddm::fail_with(FDDM_ERR_CUDA, cudaGetErrorString(ce));
+  fddm::count_launches(1);
   return FDDM_OK;
 }

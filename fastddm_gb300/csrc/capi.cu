@@ -1,4 +1,7 @@
 // C ABI entry points (declared in include/fddm_b200.h).
+#include <atomic>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 #include <cstring>
@@ -59,6 +62,31 @@ int run(int mode, const void* img, int dtype, uint64_t length, uint64_t height, 
 }  // namespace
 
 namespace fddm {
+namespace {
+std::atomic<uint64_t> g_launches{0};
+std::atomic<bool> g_timing{false};
+std::mutex g_ev_mu;
+std::map<int, StageEvents> g_events;  // per device
+}  // namespace
+
+void count_launches(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+StageEvents* stage_events() {
+  if (!g_timing.load()) return nullptr;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(g_ev_mu);
+  auto it = g_events.find(dev);
+  if (it == g_events.end()) {
+    StageEvents e{};
+    e.enabled = true;
+    for (auto& ev : e.ev)
+      if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
+    it = g_events.emplace(dev, e).first;
+  }
+  return &it->second;
+}
+
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 int fail_with(int code, const std::string& msg) { return fail(code, msg); }
 }  // namespace fddm
@@ -106,5 +134,24 @@ int fddm_b200_ddm_diff(const void* d_img_seq, int dtype, uint64_t length, uint64
   return run(fddm::MODE_DIFF, d_img_seq, dtype, length, height, width, lags, nlags, nx, ny, 0, d_window, d_out,
              d_workspace, workspace_bytes, precision, stream);
 }
+
+int fddm_b200_set_stage_timing(int enable) {
+  fddm::g_timing.store(enable != 0);
+  return FDDM_OK;
+}
+
+int fddm_b200_stage_times(float* spatial_ms, float* temporal_ms) {
+  g_last_error.clear();
+  if (!spatial_ms || !temporal_ms) return fail(FDDM_ERR_INVALID, "null pointer argument");
+  fddm::StageEvents* e = fddm::stage_events();
+  if (!e) return fail(FDDM_ERR_INVALID, "stage timing is not enabled");
+  cudaError_t ce = cudaEventSynchronize(e->ev[2]);
+  if (ce == cudaSuccess) ce = cudaEventElapsedTime(spatial_ms, e->ev[0], e->ev[1]);
+  if (ce == cudaSuccess) ce = cudaEventElapsedTime(temporal_ms, e->ev[1], e->ev[2]);
+  if (ce != cudaSuccess) return fail(FDDM_ERR_CUDA, cudaGetErrorString(ce));
+  return FDDM_OK;
+}
+
+uint64_t fddm_b200_launch_count(void) { return fddm::g_launches.load(); }
 
 }  // extern "C"

@@ -95,6 +95,10 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     }
   }
 
+  StageEvents* evs = stage_events();
+  if (evs) cudaEventRecord(evs->ev[0], st);
+  int launches = r.window ? 1 : 0;
+
   // stages 1-2 over frame chunks
   SpatialArgs sa{};
   sa.img = r.img;
@@ -123,7 +127,9 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     dim3 gc((nkx + L.cols_per_block - 1) / L.cols_per_block, (sa.tc + L.frames_per_block - 1) / L.frames_per_block);
     k_cols<S><<<gc, 256, smem_cols, st>>>(sa);
     if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+    launches += 2;
   }
+  if (evs) cudaEventRecord(evs->ev[1], st);
 
   // stage 3
   TemporalArgs ta{};
@@ -150,6 +156,8 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   if (r.mode == MODE_FFT) k_tfft<S, A><<<grid, threads, smem_t, st>>>(ta);
   else k_tdiff<S, A><<<grid, threads, smem_t, st>>>(ta);
   if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+  if (evs) cudaEventRecord(evs->ev[2], st);
+  count_launches(launches + 1);
   return 0;
 }
 

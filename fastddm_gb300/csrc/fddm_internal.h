@@ -81,6 +81,15 @@ struct WorkLayout {
 void set_last_error(const std::string& msg);
 int fail_with(int code, const std::string& msg);
 
+// Diagnostics: kernel launch counter and optional stage events.
+void count_launches(int n);
+struct StageEvents {
+  bool enabled;
+  cudaEvent_t ev[3];
+};
+// Events of the calling device when stage timing is enabled, else nullptr.
+StageEvents* stage_events();
+
 // Element size of the spectrum for a precision tier.
 size_t spec_elem_bytes(int precision);
 // Plan the workspace; returns false with a message when the problem is unsupported.

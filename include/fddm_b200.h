@@ -122,6 +122,17 @@ int fddm_b200_azimuthal_average(const double* d_data, uint64_t nrows, uint64_t n
                                 const double* d_weight, const double* d_sumw, const double* d_bias,
                                 double* d_avg, double* d_err, void* stream);
 
+/* Diagnostics (no counterpart in the reference, which has no tracing).
+   fddm_b200_set_stage_timing(1) makes every following ddm call record CUDA
+   events on its stream around the spatial stage (row and column FFT passes)
+   and the temporal stage; fddm_b200_stage_times waits for the last call's
+   events and returns the two durations in milliseconds.
+   fddm_b200_launch_count returns the number of kernels this library has
+   launched in the process so far. */
+int fddm_b200_set_stage_timing(int enable);
+int fddm_b200_stage_times(float* spatial_ms, float* temporal_ms);
+uint64_t fddm_b200_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif

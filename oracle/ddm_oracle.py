@@ -110,6 +110,45 @@ def ddm_diff(img_seq: np.ndarray, lags: Iterable[int], nx: int, ny: int,
 
 
 # ---------------------------------------------------------------------------
+# accuracy reference: the same quantities without cancellation
+# ---------------------------------------------------------------------------
+def ddm_exact(img_seq: np.ndarray, lags: Iterable[int], nx: int, ny: int,
+              window: Optional[np.ndarray] = None) -> np.ndarray:
+    """D, PS and VAR in extended precision (numpy long double where its FFT supports it).
+
+    D(lag) = <|F(t+lag) - F(t)|^2>_t by direct differences (the diff-mode
+    definition, src/cpp/ddm.cc:118-146), PS = <|F|^2>_t, VAR = <|F - <F>_t|^2>_t
+    (the variance the reference computes as PS - |<F>|^2, ddm.cc:149-164).  Both
+    reference algorithms lose digits to cancellation where D or VAR is small
+    next to PS (fft mode: S1 + S2 - 2 Re C; VAR: PS - |<F>|^2); this one does
+    not, so it is the yardstick for the error of every algorithm.
+    """
+    lags = [int(l) for l in lags]
+    T, H, W = img_seq.shape
+    ld = np.longdouble
+    try:
+        probe = np.fft.rfft2(np.ones((2, 2), dtype=ld))
+        ext = probe.dtype.itemsize > 16
+    except TypeError:  # pragma: no cover - numpy without long double FFTs
+        ext = False
+    dt = ld if ext else np.float64
+    buf = np.zeros((T, ny, nx), dtype=dt)
+    buf[:, :H, :W] = img_seq.astype(dt)
+    if window is not None and np.size(window) > 0:
+        buf[:, :H, :W] *= np.asarray(window).astype(dt)
+    F = np.fft.rfft2(buf, axes=(1, 2)) / np.sqrt(dt(nx * ny))
+    Fq = F.reshape(T, -1)
+    out = np.empty((len(lags) + 2, Fq.shape[1]), dtype=dt)
+    for i, lag in enumerate(lags):
+        d = Fq[lag:] - Fq[: T - lag]
+        out[i] = (d.real * d.real + d.imag * d.imag).sum(axis=0) / dt(T - lag)
+    out[-2] = (Fq.real * Fq.real + Fq.imag * Fq.imag).sum(axis=0) / dt(T)
+    G = Fq - Fq.sum(axis=0) / dt(T)
+    out[-1] = (G.real * G.real + G.imag * G.imag).sum(axis=0) / dt(T)
+    return shift_y(out.reshape(len(lags) + 2, ny, nx // 2 + 1)).astype(np.float64)
+
+
+# ---------------------------------------------------------------------------
 # front door pieces: src/python/_ddm.py:128-198, _fftopt.py:29-150
 # ---------------------------------------------------------------------------
 def next_fast_len_cpp(target: int) -> int:
@@ -229,16 +268,24 @@ def azimuthal_average(data: np.ndarray, kx: np.ndarray, ky: np.ndarray, width: i
 # ---------------------------------------------------------------------------
 # error metrics used by the tests and the bench report
 # ---------------------------------------------------------------------------
-def rel_err(test: np.ndarray, ref: np.ndarray, skip_dc: bool = False, ny: Optional[int] = None) -> float:
+def rel_err(test: np.ndarray, ref: np.ndarray, skip_dc: bool = False, ny: Optional[int] = None,
+            floor: float = 0.0) -> float:
     """Max elementwise |test - ref| / |ref| over the structure-function rows.
 
-    With ``skip_dc`` the q = 0 mode (row ny//2, column 0 after the y shift) is excluded.
+    With ``skip_dc`` the q = 0 mode (row ny//2, column 0 after the y shift) is
+    excluded.  ``floor`` > 0 measures entries smaller than ``floor`` times the
+    largest |ref| of their row against that threshold instead (for values that
+    are exactly zero in exact arithmetic).
     """
     t = np.asarray(test, dtype=np.float64)
     r = np.asarray(ref, dtype=np.float64)
+    den = np.abs(r)
+    if floor > 0 and r.ndim >= 2:
+        rowmax = np.max(np.abs(r).reshape(r.shape[0], -1), axis=1).reshape((-1,) + (1,) * (r.ndim - 1))
+        den = np.maximum(den, floor * rowmax)
     with np.errstate(divide="ignore", invalid="ignore"):
-        e = np.abs(t - r) / np.abs(r)
-    e = np.where(r == 0, np.where(t == 0, 0.0, np.inf), e)
+        e = np.abs(t - r) / den
+    e = np.where(den == 0, np.where(t == r, 0.0, np.inf), e)
     if skip_dc:
         ny = ny if ny is not None else r.shape[-2]
         e = e.copy()
