@@ -30,17 +30,19 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 CONFIGS = {
-    # name: (scene attribute, lags builder, mode)
-    "large": "CONFIG3",
-    "medium": "CONFIG2",
-    "small": "CONFIG1",
+    # name: scene in fastddm_gb300.synthetic
+    "large": "CONFIG3",        # 4000 x 1024^2 uint8, 200 log lags (the headline workload)
+    "medium": "CONFIG2",       # 512 x 512^2 uint16, all lags, Blackman-Harris window
+    "small": "CONFIG1",        # 64 x 128^2 uint16, all lags
+    "large_tall": "CONFIG3_TALL",  # profiling: the large workload's temporal kernel on 64^2 frames
+    "large_wide": "CONFIG3_WIDE",  # profiling: the large workload's spatial kernels on 64 frames
 }
 
 
 def lags_for(name: str, T: int) -> np.ndarray:
     from fastddm_gb300 import lags as lg
 
-    if name == "large":
+    if name in ("large", "large_tall"):
         return np.unique(lg.logspace_int(T - 1, num=200, endpoint=True))
     return np.arange(1, T)
 

@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
         if (win) vb = sc<S>::mul(vb, win[(size_t)(y0 + 1) * W + x]);
       }
     }
-    buf[p * nx + x] = {va, vb};
+    buf[swz<S>(p * nx + x)] = {va, vb};
   }
   __syncthreads();
   fft_forward<S>(buf, np, nx, a.px, reinterpret_cast<const cx<S>*>(a.twx), tid, nthr);
@@ -186,8 +186,8 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
     const int k = e / ny2;
     const int yl = e - k * ny2;
     const int p = yl >> 1;
-    const cx<S> zk = buf[p * nx + a.permx[k]];
-    const cx<S> zn = buf[p * nx + a.permx[k == 0 ? 0 : nx - k]];
+    const cx<S> zk = buf[swz<S>(p * nx + a.permx[k])];
+    const cx<S> zn = buf[swz<S>(p * nx + a.permx[k == 0 ? 0 : nx - k])];
     cx<S> v;
     if ((yl & 1) == 0) {
       v = {sc<S>::half(sc<S>::add(zk.r, zn.r)), sc<S>::half(sc<S>::sub(zk.i, zn.i))};
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(256) k_cols(SpatialArgs a) {
     const int kc = c - tl * CK;
     cx<S> v = czero<S>();
     if (kc < nk && tl < ntg && y < H) v = R[((size_t)(tl0 + tl) * nkx + kc0 + kc) * a.Hpad + y];
-    buf[c * ny + y] = v;
+    buf[swz<S>(c * ny + y)] = v;
   }
   __syncthreads();
   fft_forward<S>(buf, NB, ny, a.py, reinterpret_cast<const cx<S>*>(a.twy), tid, nthr);
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(256) k_cols(SpatialArgs a) {
     const int kc = rest % CK;
     const int ky = rest / CK;
     if (tl < ntg && kc < nk) {
-      const cx<S> v = cscale(buf[(tl * CK + kc) * ny + a.permy[ky]], norm);
+      const cx<S> v = cscale(buf[swz<S>((tl * CK + kc) * ny + a.permy[ky])], norm);
       int ys = ky + half;
       if (ys >= ny) ys -= ny;
       const size_t q = (size_t)ys * nkx + kc0 + kc;
@@ -264,32 +264,64 @@ template <> struct cvt<double, double> {
 };
 
 // ---------------------------------------------------------------------------
-// Stage 3 (fft mode)
-// dynamic smem: nt * cx<S>  +  (T + 1) * A  +  96 * A (reduction scratch)
+// Stage 3 (fft mode), one q per CTA iteration:
+//   G = F - <F>_t (D is unchanged by a time-constant offset; VAR = <|G|^2>)
+//   S1(lag) + S2(lag) from prefix sums of |G|^2, kept only at the indices the
+//   lags need
+//   X = FFT_N(G zero-padded), P = |X|^2 (real)
+//   Re C(lag) = (1/N) Re DFT_N(P)(lag) (cos is even, so the forward transform
+//   serves), evaluated through one half-length complex FFT of
+//   z[m] = P(2m) + i P(2m+1) and a per-lag post-process, only at the lags
+//   D(lag) = (S1 + S2 - 2 Re C) / (T - lag)
+// Lags with T - lag <= kDirect are summed directly from the saved first and
+// last kDirect values of G: there the Wiener-Khinchin form would amplify its
+// rounding error by T / (T - lag).
+// Shared memory (see temporal_smem): buf (N), z (N/2), head, tail (kDirect
+// each), reduction scratch, the lag slot tables (int16, loaded once per CTA)
+// and, when they fit, the needed prefix sums (else per-CTA global scratch).
 // ---------------------------------------------------------------------------
+constexpr int kDirect = 32;
+
 template <class S, class A>
 __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int T = a.T, nt = a.nt, nl = a.nlags;
+  const int T = a.T, N = a.nt, N2 = a.nt / 2, nl = a.nlags;
   cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
-  A* pfx = reinterpret_cast<A*>(smem_raw + (size_t)nt * sizeof(cx<S>));
-  A* scratch = pfx + (T + 1);
+  cx<S>* z = buf + swz_round<S>(N);
+  cx<S>* head = z + swz_round<S>(N2);
+  cx<S>* tail = head + kDirect;
+  A* scratch = reinterpret_cast<A*>(tail + kDirect);
+  short* slotA = reinterpret_cast<short*>(scratch + 96);
+  short* slotB = slotA + (T + 1);
+  A* need = a.need_in_smem
+                ? reinterpret_cast<A*>(smem_raw + ((reinterpret_cast<unsigned char*>(slotB + (T + 1)) - smem_raw + 15) & ~15))
+                : reinterpret_cast<A*>(a.need) + (size_t)blockIdx.x * (2 * nl + 2);
   const int tid = threadIdx.x, nthr = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
   const cx<S>* F = reinterpret_cast<const cx<S>*>(a.spec);
   const cx<S>* tw = reinterpret_cast<const cx<S>*>(a.twt);
+  const cx<S>* tw2 = reinterpret_cast<const cx<S>*>(a.twt2);
+  const int* iperm = a.ipermt;
+  const int* perm2 = a.permt2;
   const A invT = sc<A>::cst(a.invT_h, a.invT_l, a.invT_d);
-  const A invnt = sc<A>::cst(a.invnt_h, a.invnt_l, a.invnt_d);
+  const A invN = sc<A>::cst(a.invnt_h, a.invnt_l, a.invnt_d);
   const int chunk = (T + nthr - 1) / nthr;
+  const int tail0 = T - kDirect;  // first index kept in `tail` (may be negative)
+
+  for (int t = tid; t <= T; t += nthr) {
+    slotA[t] = (short)a.slotA[t];
+    slotB[t] = (short)a.slotB[t];
+  }
+  __syncthreads();
 
   for (size_t q = blockIdx.x; q < a.Q; q += gridDim.x) {
     const cx<S>* src = F + q * a.Tpad;
-    for (int t = tid; t < nt; t += nthr) buf[t] = t < T ? src[t] : czero<S>();
+    for (int t = tid; t < N; t += nthr) buf[swz<S>(t)] = t < T ? src[t] : czero<S>();
     __syncthreads();
 
-    // sums of F and |F|^2
     A v[3] = {sc<A>::zero(), sc<A>::zero(), sc<A>::zero()};
     for (int t = tid; t < T; t += nthr) {
-      const cx<S> f = buf[t];
+      const cx<S> f = buf[swz<S>(t)];
       const A fr = cvt<S, A>::to_acc(f.r), fi = cvt<S, A>::to_acc(f.i);
       v[0] = sc<A>::add(v[0], fr);
       v[1] = sc<A>::add(v[1], fi);
@@ -300,44 +332,79 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
     const A ps = sc<A>::mul(v[2], invT);
     const S msr = cvt<S, A>::to_fft(mr), msi = cvt<S, A>::to_fft(mi);
 
-    // G = F - <F>; prefix sums of |G|^2 over a contiguous chunk per thread
+    // G = F - <F>; |G|^2 summed over a contiguous chunk per thread
     const int t_beg = min(T, tid * chunk), t_end = min(T, t_beg + chunk);
     A run = sc<A>::zero();
     for (int t = t_beg; t < t_end; ++t) {
-      cx<S> g = buf[t];
+      cx<S> g = buf[swz<S>(t)];
       g.r = sc<S>::sub(g.r, msr);
       g.i = sc<S>::sub(g.i, msi);
-      buf[t] = g;
+      buf[swz<S>(t)] = g;
+      if (t < kDirect) head[t] = g;
+      if (t >= tail0) tail[t - tail0] = g;
       run = sc<A>::add(run, sc<A>::sqsum(cvt<S, A>::to_acc(g.r), cvt<S, A>::to_acc(g.i)));
-      pfx[t + 1] = run;
     }
     A total;
-    const A off = block_exclusive_scan<A>(run, scratch, total);
-    for (int t = t_beg; t < t_end; ++t) pfx[t + 1] = sc<A>::add(pfx[t + 1], off);
-    if (tid == 0) pfx[0] = sc<A>::zero();
+    A pre = block_exclusive_scan<A>(run, scratch, total);
+    // prefix sums pfx[t + 1] = sum_{s <= t} |G(s)|^2, stored at the slots the lags need
+    for (int t = t_beg; t < t_end; ++t) {
+      const cx<S> g = buf[swz<S>(t)];
+      pre = sc<A>::add(pre, sc<A>::sqsum(cvt<S, A>::to_acc(g.r), cvt<S, A>::to_acc(g.i)));
+      const int sa = slotA[t + 1], sb = slotB[t + 1];
+      if (sa >= 0) need[sa] = pre;
+      if (sb >= 0) need[nl + sb] = pre;
+    }
+    if (tid == 0 && slotB[0] >= 0) need[nl + slotB[0]] = sc<A>::zero();
     __syncthreads();
 
-    // autocorrelation via zero-padded FFT: C(tau) = IFFT(|FFT(G)|^2)(tau) / nt
-    fft_forward<S>(buf, 1, nt, a.pt, tw, tid, nthr);
-    for (int k = tid; k < nt; k += nthr) {
-      const cx<S> x = buf[k];
-      buf[k] = {sc<S>::sqsum(x.r, x.i), sc<S>::zero()};
+    fft_forward<S>(buf, 1, N, a.pt, tw, tid, nthr);
+    // P(k) = |X(k)|^2 scattered into z as the real sequence z[k/2].{r,i}
+    for (int p = tid; p < N; p += nthr) {
+      const cx<S> x = buf[swz<S>(p)];
+      const int k = iperm[p];
+      const S pv = sc<S>::sqsum(x.r, x.i);
+      cx<S>* e = &z[swz<S>(k >> 1)];
+      if (k & 1) e->i = pv;
+      else e->r = pv;
     }
     __syncthreads();
-    fft_inverse<S>(buf, 1, nt, a.pt, tw, tid, nthr);
+    fft_forward<S>(z, 1, N2, a.pt2, tw2, tid, nthr);
 
-    const A tot = pfx[T];
     for (int l = tid; l < nl; l += nthr) {
       const int tau = a.lags[l];
-      const A c = sc<A>::mul(cvt<S, A>::to_acc(buf[tau].r), invnt);
-      // S1 + S2 - 2 C = pfx[T - tau] + (pfx[T] - pfx[tau]) - 2 C
-      A num = sc<A>::add(pfx[T - tau], sc<A>::sub(tot, pfx[tau]));
-      num = sc<A>::sub(num, sc<A>::add(c, c));
+      if (T - tau <= kDirect) continue;
+      const cx<S> zk = z[swz<S>(perm2[tau])];
+      const cx<S> zn = z[swz<S>(perm2[tau == 0 ? 0 : N2 - tau])];
+      // DFT_N(P)(tau) = Xe + w^tau Xo with Xe = (Zk + conj Zn)/2, Xo = (Zk - conj Zn)/(2i);
+      // y is twice its real part
+      const S xe = sc<S>::add(zk.r, zn.r);
+      const cx<S> xo = {sc<S>::add(zk.i, zn.i), sc<S>::sub(zn.r, zk.r)};
+      const cx<S> w = tw[tau];
+      const S y = sc<S>::add(xe, sc<S>::sub(sc<S>::mul(w.r, xo.r), sc<S>::mul(w.i, xo.i)));
+      // 2 Re C = y / N
+      const A c2 = sc<A>::mul(cvt<S, A>::to_acc(y), invN);
+      A num = sc<A>::add(need[l], sc<A>::sub(total, need[nl + l]));
+      num = sc<A>::sub(num, c2);
       a.out[(size_t)l * a.Q + q] = sc<A>::to_double(num) * a.rcp[l];
+    }
+    // the last lags: direct differences
+    for (int l = nl - 1 - warp; l >= 0; l -= nw) {
+      const int tau = a.lags[l];
+      const int m = T - tau;
+      if (m > kDirect) break;
+      A acc = sc<A>::zero();
+      for (int t = lane; t < m; t += 32) {
+        const cx<S> g1 = tail[t + tau - tail0], g0 = head[t];
+        const A dr = sc<A>::sub(cvt<S, A>::to_acc(g1.r), cvt<S, A>::to_acc(g0.r));
+        const A di = sc<A>::sub(cvt<S, A>::to_acc(g1.i), cvt<S, A>::to_acc(g0.i));
+        acc = sc<A>::add(acc, sc<A>::sqsum(dr, di));
+      }
+      acc = warp_sum(acc);
+      if (lane == 0) a.out[(size_t)l * a.Q + q] = sc<A>::to_double(acc) * a.rcp[l];
     }
     if (tid == 0) {
       a.out[(size_t)nl * a.Q + q] = sc<A>::to_double(ps);
-      a.out[(size_t)(nl + 1) * a.Q + q] = sc<A>::to_double(sc<A>::mul(tot, invT));
+      a.out[(size_t)(nl + 1) * a.Q + q] = sc<A>::to_double(sc<A>::mul(total, invT));
     }
     __syncthreads();
   }

@@ -24,10 +24,12 @@ template <class K> inline cudaError_t allow_smem(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-template <class S, class A>
-size_t temporal_smem(int mode, int T, int nt) {
-  if (mode == MODE_FFT) return (size_t)nt * sizeof(cx<S>) + (size_t)(T + 1) * sizeof(A) + 96 * sizeof(A);
-  return (size_t)T * sizeof(cx<S>) + 96 * sizeof(A);
+// Threads per CTA of the temporal kernels: about one radix-8 butterfly per
+// thread and pass, so that short transforms run several CTAs per SM.
+inline int temporal_threads(int n) {
+  int t = 128;
+  while (t < 512 && t * 8 < n) t *= 2;
+  return t;
 }
 
 template <class S, class IN>
@@ -68,9 +70,10 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   const int nl = (int)r.lags.size();
   unsigned char* ws = static_cast<unsigned char*>(r.work);
 
-  FftTables tx, ty, tt;
+  FftTables tx, ty, tt, tt2;
   if (!get_tables(nx, kind, tx, err) || !get_tables(ny, kind, ty, err)) return 3;
-  if (r.mode == MODE_FFT && !get_tables((int)r.nt, kind, tt, err)) return 3;
+  const int N = L.nt_fft;
+  if (r.mode == MODE_FFT && (!get_tables(N, kind, tt, err) || !get_tables(N / 2, kind, tt2, err))) return 3;
 
   cudaError_t ce;
   // window in the FFT scalar type
@@ -90,6 +93,19 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   if (nl > 0) {
     if ((ce = cudaMemcpyAsync(d_lags, r.lags.data(), nl * sizeof(int), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
         (ce = cudaMemcpyAsync(d_rcp, rcp.data(), nl * sizeof(double), cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+      err = cudaGetErrorString(ce);
+      return 3;
+    }
+  }
+  // slot tables of the prefix sums each lag needs: pfx[T - lag] (A) and pfx[lag] (B)
+  int* d_slots = reinterpret_cast<int*>(ws + L.slot_off);
+  if (r.mode == MODE_FFT) {
+    std::vector<int> slots(2 * (size_t)(T + 1), -1);
+    for (int l = 0; l < nl; ++l) {
+      slots[T - r.lags[l]] = l;
+      slots[(size_t)(T + 1) + r.lags[l]] = l;
+    }
+    if ((ce = cudaMemcpyAsync(d_slots, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, st)) != cudaSuccess) {
       err = cudaGetErrorString(ce);
       return 3;
     }
@@ -116,8 +132,8 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   split_ff(norm, sa.norm_h, sa.norm_l);
   sa.norm_d = norm;
   const int npairs = (H + 1) / 2;
-  const size_t smem_rows = (size_t)L.pairs_per_block * nx * sizeof(cx<S>);
-  const size_t smem_cols = (size_t)L.cols_per_block * L.frames_per_block * ny * sizeof(cx<S>);
+  const size_t smem_rows = (size_t)swz_round<S>(L.pairs_per_block * nx) * sizeof(cx<S>);
+  const size_t smem_cols = (size_t)swz_round<S>(L.cols_per_block * L.frames_per_block * ny) * sizeof(cx<S>);
   if ((ce = allow_smem(k_cols<S>, smem_cols)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
   for (int t0 = 0; t0 < T; t0 += L.chunk) {
     sa.t0 = t0;
@@ -134,16 +150,26 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   // stage 3
   TemporalArgs ta{};
   ta.spec = ws + L.spec_off;
-  ta.Q = Q; ta.Tpad = L.Tpad; ta.T = T; ta.nt = (int)r.nt; ta.nlags = nl;
-  if (r.mode == MODE_FFT) { ta.pt = tt.plan; ta.twt = tt.tw; }
+  ta.Q = Q; ta.Tpad = L.Tpad; ta.T = T; ta.nt = N; ta.nlags = nl;
+  size_t smem_t = (size_t)T * sizeof(cx<S>) + 96 * sizeof(A);
+  int threads = temporal_threads(T);
+  if (r.mode == MODE_FFT) {
+    ta.pt = tt.plan; ta.twt = tt.tw; ta.ipermt = tt.iperm;
+    ta.pt2 = tt2.plan; ta.twt2 = tt2.tw; ta.permt2 = tt2.perm;
+    ta.slotA = d_slots; ta.slotB = d_slots + (T + 1);
+    ta.need = ws + L.need_off;
+    const size_t with_need = temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), true);
+    ta.need_in_smem = with_need <= kSmemLimit ? 1 : 0;
+    smem_t = temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), ta.need_in_smem != 0);
+    split_ff(1.0 / (double)N, ta.invnt_h, ta.invnt_l);
+    ta.invnt_d = 1.0 / (double)N;
+    threads = temporal_threads(N);
+  }
   ta.lags = d_lags; ta.rcp = d_rcp; ta.out = r.out;
   split_ff(1.0 / (double)T, ta.invT_h, ta.invT_l); ta.invT_d = 1.0 / (double)T;
-  if (r.mode == MODE_FFT) { split_ff(1.0 / (double)r.nt, ta.invnt_h, ta.invnt_l); ta.invnt_d = 1.0 / (double)r.nt; }
-  const size_t smem_t = temporal_smem<S, A>(r.mode, T, (int)r.nt);
   int dev = 0, nsm = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int threads = 512;
   if (r.mode == MODE_FFT) {
     if ((ce = allow_smem(k_tfft<S, A>, smem_t)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tfft<S, A>, threads, smem_t);
@@ -152,7 +178,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tdiff<S, A>, threads, smem_t);
   }
   if (occ < 1) { err = "temporal kernel does not fit on an SM (shared memory " + std::to_string(smem_t) + " B)"; return 4; }
-  const unsigned grid = (unsigned)std::min<size_t>(Q, (size_t)occ * nsm);
+  const unsigned grid = (unsigned)std::min<size_t>(std::min<size_t>(Q, (size_t)occ * nsm), kMaxTemporalCtas);
   if (r.mode == MODE_FFT) k_tfft<S, A><<<grid, threads, smem_t, st>>>(ta);
   else k_tdiff<S, A><<<grid, threads, smem_t, st>>>(ta);
   if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }

@@ -38,9 +38,16 @@ struct SpatialArgs {
 struct TemporalArgs {
   const void* spec;
   size_t Q;
-  int Tpad, T, nt, nlags;
-  FftPlan pt;
+  int Tpad, T, nt, nlags;  // nt: the temporal transform length N chosen by plan_layout
+  FftPlan pt, pt2;         // plans for N and N/2
   const void* twt;
+  const void* twt2;
+  const int* ipermt;      // position -> natural index after the length-N forward FFT
+  const int* permt2;      // natural index -> position after the length-N/2 forward FFT
+  const int* slotA;      // (T + 1): lag index l with T - lag_l == t, or -1
+  const int* slotB;      // (T + 1): lag index l with lag_l == t, or -1
+  void* need;            // per-CTA scratch, (2 * nlags + 2) accumulators per CTA
+  int need_in_smem;      // 1: the needed prefix sums live in shared memory instead
   const int* lags;       // device, nlags
   const double* rcp;     // device, 1/(T - lag)
   double* out;           // (nlags + 2, Q)
@@ -72,10 +79,22 @@ struct WorkLayout {
   size_t spec_off, spec_bytes;
   size_t rbuf_off, rbuf_bytes;
   size_t win_off, win_bytes;
-  size_t lags_off, rcp_off;
+  size_t lags_off, rcp_off, slot_off, need_off;
   size_t total;
   int Tpad, Hpad, chunk, pairs_per_block, cols_per_block, frames_per_block;
+  int nt_fft;  // temporal transform length actually used (fft mode)
 };
+
+// Upper bound on the temporal kernel's grid (sizes its per-CTA scratch).
+constexpr int kMaxTemporalCtas = 1024;
+
+// Cheapest even length >= 2T - 1 for the temporal transform (fft mode).
+int choose_temporal_length(int64_t T);
+
+// Shared memory of the fft-mode temporal kernel for element sizes es (FFT
+// scalar complex) and ea (accumulator); `need_in_smem` selects the layout.
+size_t temporal_fft_smem(int T, int N, int nlags, size_t es, size_t ea, bool need_in_smem);
+constexpr size_t kSmemLimit = 232448;  // 227 KB opt-in per CTA
 
 // Thread-local error message reported by fddm_b200_last_error().
 void set_last_error(const std::string& msg);
@@ -106,7 +125,8 @@ int run_ddm_f32(const DdmRequest& r, cudaStream_t st, std::string& err);
 struct FftTables {
   FftPlan plan;
   const void* tw;
-  const int* perm;
+  const int* perm;   // natural index -> position after the forward FFT
+  const int* iperm;  // position -> natural index
 };
 // kind: 0 = ff (16 B twiddles), 1 = double, 2 = float
 bool get_tables(int n, int kind, FftTables& out, std::string& err);

@@ -130,7 +130,26 @@ template <class S, int R, bool INV> __device__ __forceinline__ void dft(cx<S>* v
 }
 
 // ---------------------------------------------------------------------------
-// One in-place pass over `nfft` transforms of length n, stored at buf + f*ld.
+// Shared-memory swizzle.  A warp's 16-byte (8-byte) accesses are served in
+// phases of 8 (16) lanes, one 128-byte bank row per phase, so lanes of a phase
+// must touch distinct element slots modulo G = 128 / sizeof(element).  The
+// butterflies access runs of consecutive elements (stride >= G passes) or
+// elements G apart (the last passes); XOR-ing the slot with the row number
+// serves both without conflicts.  The map only permutes within aligned groups
+// of G elements, so buffers are sized to a multiple of G.
+// ---------------------------------------------------------------------------
+template <class S> struct swz_group { static constexpr int G = 128 / (int)sizeof(cx<S>); };
+template <class S> __device__ __forceinline__ int swz(int i) {
+  constexpr int G = swz_group<S>::G;
+  return i ^ ((i / G) & (G - 1));
+}
+template <class S> __host__ __device__ constexpr int swz_round(int n) {
+  return (n + swz_group<S>::G - 1) / swz_group<S>::G * swz_group<S>::G;
+}
+
+// ---------------------------------------------------------------------------
+// One in-place pass over `nfft` transforms of length n, stored at logical
+// offset f*ld of the (swizzled) buffer.
 // ---------------------------------------------------------------------------
 template <class S, int R, bool INV>
 __device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int ld, int n, int M,
@@ -144,10 +163,10 @@ __device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int 
     const int loc = beta - f * bpf;
     const int blk = loc / stride;
     const int j = loc - blk * stride;
-    cx<S>* p = buf + (size_t)f * ld + blk * M + j;
+    const int base = f * ld + blk * M + j;
     cx<S> v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = p[r * stride];
+    for (int r = 0; r < R; ++r) v[r] = buf[swz<S>(base + r * stride)];
     if (!INV) {
       dft<S, R, false>(v);
       if (j != 0) {
@@ -162,7 +181,7 @@ __device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int 
       dft<S, R, true>(v);
     }
 #pragma unroll
-    for (int r = 0; r < R; ++r) p[r * stride] = v[r];
+    for (int r = 0; r < R; ++r) buf[swz<S>(base + r * stride)] = v[r];
   }
 }
 

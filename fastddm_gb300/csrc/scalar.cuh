@@ -156,6 +156,28 @@ template <class S> __device__ __forceinline__ cx<S> cmulc(cx<S> a, cx<S> b) {
   return {sc<S>::add(sc<S>::mul(a.r, b.r), sc<S>::mul(a.i, b.i)),
           sc<S>::sub(sc<S>::mul(a.i, b.r), sc<S>::mul(a.r, b.i))};
 }
+// float-float complex products with one renormalisation per component:
+// the two leading products are split exactly (TwoProd), their difference is
+// an exact TwoSum, and all low-order terms are folded into one FMA chain.
+__device__ __forceinline__ ff ff_dot2(ff a, ff b, ff c, ff d, float sgn) {  // a*b + sgn*c*d
+  const float p1 = __fmul_rn(a.h, b.h), e1 = __fmaf_rn(a.h, b.h, -p1);
+  const float ch = __fmul_rn(sgn, c.h), cl = __fmul_rn(sgn, c.l);
+  const float p2 = __fmul_rn(ch, d.h), e2 = __fmaf_rn(ch, d.h, -p2);
+  const ff s = two_sum(p1, p2);
+  float lo = __fadd_rn(__fadd_rn(e1, e2), s.l);
+  lo = __fmaf_rn(a.h, b.l, lo);
+  lo = __fmaf_rn(a.l, b.h, lo);
+  lo = __fmaf_rn(ch, d.l, lo);
+  lo = __fmaf_rn(cl, d.h, lo);
+  return fast_two_sum(s.h, lo);
+}
+template <> __device__ __forceinline__ cx<ff> cmul<ff>(cx<ff> a, cx<ff> b) {
+  return {ff_dot2(a.r, b.r, a.i, b.i, -1.0f), ff_dot2(a.r, b.i, a.i, b.r, 1.0f)};
+}
+template <> __device__ __forceinline__ cx<ff> cmulc<ff>(cx<ff> a, cx<ff> b) {
+  return {ff_dot2(a.r, b.r, a.i, b.i, 1.0f), ff_dot2(a.i, b.r, a.r, b.i, -1.0f)};
+}
+
 template <class S> __device__ __forceinline__ cx<S> cscale(cx<S> a, S s) {
   return {sc<S>::mul(a.r, s), sc<S>::mul(a.i, s)};
 }

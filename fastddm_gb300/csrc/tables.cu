@@ -51,6 +51,7 @@ struct Entry {
   FftPlan plan;
   void* tw = nullptr;
   int* perm = nullptr;
+  int* iperm = nullptr;
 };
 std::mutex g_mu;
 std::map<std::tuple<int, int, int>, Entry> g_cache;  // (device, n, kind)
@@ -70,8 +71,9 @@ bool get_tables(int n, int kind, FftTables& out, std::string& err) {
       err = "length " + std::to_string(n) + " has a prime factor other than 2, 3, 5, 7, 11, 13";
       return false;
     }
-    std::vector<int> perm(n);
+    std::vector<int> perm(n), iperm(n);
     for (int k = 0; k < n; ++k) perm[k] = perm_of(e.plan, k);
+    for (int k = 0; k < n; ++k) iperm[perm[k]] = k;
     const size_t esz = kind == 2 ? 8 : 16;
     std::vector<unsigned char> tw(esz * (size_t)n);
     for (int k = 0; k < n; ++k) {
@@ -93,11 +95,14 @@ bool get_tables(int n, int kind, FftTables& out, std::string& err) {
     }
     if ((ce = cudaMalloc(&e.tw, tw.size())) != cudaSuccess ||
         (ce = cudaMalloc(reinterpret_cast<void**>(&e.perm), sizeof(int) * n)) != cudaSuccess ||
+        (ce = cudaMalloc(reinterpret_cast<void**>(&e.iperm), sizeof(int) * n)) != cudaSuccess ||
         (ce = cudaMemcpy(e.tw, tw.data(), tw.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (ce = cudaMemcpy(e.perm, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        (ce = cudaMemcpy(e.perm, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (ce = cudaMemcpy(e.iperm, iperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice)) != cudaSuccess) {
       err = std::string("FFT table upload failed: ") + cudaGetErrorString(ce);
       if (e.tw) cudaFree(e.tw);
       if (e.perm) cudaFree(e.perm);
+      if (e.iperm) cudaFree(e.iperm);
       return false;
     }
     it = g_cache.emplace(key, e).first;
@@ -105,7 +110,59 @@ bool get_tables(int n, int kind, FftTables& out, std::string& err) {
   out.plan = it->second.plan;
   out.tw = it->second.tw;
   out.perm = it->second.perm;
+  out.iperm = it->second.iperm;
   return true;
+}
+
+// Issue cost per point of one in-place pass of each radix in float-float
+// arithmetic (instruction counts of the butterfly plus its twiddles).
+static double pass_cost(int r) {
+  switch (r) {
+    case 8: return 110.0;
+    case 4: return 80.0;
+    case 2: return 45.0;
+    case 3: return 72.0;
+    case 5: return 140.0;
+    case 7: return 190.0;
+    case 11: return 300.0;
+    default: return 360.0;
+  }
+}
+
+static double fft_cost(int n) {
+  FftPlan p;
+  if (!make_plan(n, p)) return 1e300;
+  double c = 0.0;
+  for (int s = 0; s < p.npass; ++s) c += pass_cost(p.radix[s]);
+  return c * n;
+}
+
+int choose_temporal_length(int64_t T) {
+  const int64_t lo = std::max<int64_t>(2, 2 * T - 1);
+  int64_t p2 = 1;
+  while (p2 < lo) p2 <<= 1;
+  int best = (int)p2;
+  double best_cost = fft_cost(best) + fft_cost(best / 2);
+  for (int64_t n = lo; n < p2; ++n) {
+    if (n % 2) continue;
+    FftPlan p;
+    if (!make_plan((int)n, p)) continue;
+    const double c = fft_cost((int)n) + fft_cost((int)(n / 2));
+    if (c < best_cost) {
+      best_cost = c;
+      best = (int)n;
+    }
+  }
+  return best;
+}
+
+static size_t round_to(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+size_t temporal_fft_smem(int T, int N, int nlags, size_t es, size_t ea, bool need_in_smem) {
+  const size_t g = 128 / es;  // swizzle group (elements)
+  size_t b = (round_to(N, g) + round_to(N / 2, g) + 64) * es + 96 * ea + 2 * (size_t)(T + 1) * sizeof(short);
+  if (need_in_smem) b = round_to(b, 16) + (2 * (size_t)nlags + 2) * ea;
+  return b;
 }
 
 size_t spec_elem_bytes(int precision) { return precision == PREC_F32 ? 8 : 16; }
@@ -116,12 +173,15 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
   if (r.T < 1 || r.H < 1 || r.W < 1) { err = "empty image sequence"; return false; }
   if (r.nx < r.W || r.ny < r.H) { err = "nx, ny must be at least the image width and height"; return false; }
   if (r.T > (1 << 30) || r.nx > (1 << 20) || r.ny > (1 << 20)) { err = "problem too large"; return false; }
+  if (r.mode == MODE_FFT && r.T >= 32767) { err = "fft mode supports at most 32766 frames"; return false; }
   FftPlan p;
   if (!make_plan((int)r.nx, p)) { err = "nx=" + std::to_string(r.nx) + " has a prime factor other than 2, 3, 5, 7, 11, 13"; return false; }
   if (!make_plan((int)r.ny, p)) { err = "ny=" + std::to_string(r.ny) + " has a prime factor other than 2, 3, 5, 7, 11, 13"; return false; }
+  L.nt_fft = 0;
   if (r.mode == MODE_FFT) {
     if (r.nt < 2 * r.T - 1) { err = "nt must be at least 2*len(img_seq) - 1"; return false; }
-    if (!make_plan((int)r.nt, p)) { err = "nt=" + std::to_string(r.nt) + " has a prime factor other than 2, 3, 5, 7, 11, 13"; return false; }
+    // any length >= 2T - 1 gives the same linear autocorrelation; use the cheapest
+    L.nt_fft = choose_temporal_length(r.T);
   }
   for (int lag : r.lags)
     if (lag < 0 || lag >= r.T) { err = "lags must lie in [0, len(img_seq) - 1]"; return false; }
@@ -136,7 +196,7 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
   const int nb = (int)std::max<size_t>(1, target / ((size_t)r.ny * es));
   L.frames_per_block = std::min(nb, 8);
   L.cols_per_block = std::max(1, nb / L.frames_per_block);
-  if ((size_t)L.pairs_per_block * r.nx * es > 232448 || (size_t)nb * r.ny * es > 232448) {
+  if ((size_t)(L.pairs_per_block * r.nx + 16) * es > kSmemLimit || (size_t)(nb * r.ny + 16) * es > kSmemLimit) {
     err = "image dimensions too large for the shared-memory FFT";
     return false;
   }
@@ -148,9 +208,9 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
   L.chunk = chunk;
   // temporal kernel shared memory
   const size_t ea = 8;
-  const size_t smem_t = r.mode == MODE_FFT ? (size_t)r.nt * es + (size_t)(r.T + 1) * ea + 96 * ea
+  const size_t smem_t = r.mode == MODE_FFT ? temporal_fft_smem((int)r.T, L.nt_fft, (int)r.lags.size(), es, ea, false)
                                            : (size_t)r.T * es + 96 * ea;
-  if (smem_t > 232448) {
+  if (smem_t > kSmemLimit) {
     err = "sequence too long for the single-CTA temporal kernel (needs " + std::to_string(smem_t) + " B of shared memory)";
     return false;
   }
@@ -160,6 +220,9 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
   L.win_off = off; L.win_bytes = r.window ? (size_t)r.H * r.W * (es / 2) : 0; off = align_up(off + L.win_bytes, 256);
   L.lags_off = off; off = align_up(off + r.lags.size() * sizeof(int) + 4, 256);
   L.rcp_off = off; off = align_up(off + r.lags.size() * sizeof(double) + 8, 256);
+  L.slot_off = off; off = align_up(off + 2 * (size_t)(r.T + 1) * sizeof(int), 256);
+  L.need_off = off;
+  if (r.mode == MODE_FFT) off = align_up(off + (size_t)kMaxTemporalCtas * (2 * r.lags.size() + 2) * ea, 256);
   L.total = off;
   return true;
 }

@@ -41,6 +41,10 @@ CONFIG1 = Scene(64, 128, 128, 200, 2.0, 2000.0, 0.5, 500.0, 0.0, "uint16", 0)
 CONFIG2 = Scene(512, 512, 512, 2000, 2.0, 2000.0, 0.2, 500.0, 0.0, "uint16", 0)
 # 8-bit large stack: offset and amplitude chosen for the 0..255 range
 CONFIG3 = Scene(4000, 1024, 1024, 5000, 1.5, 150.0, 1.0, 20.0, 0.05, "uint8", 0)
+# small cases with the kernel configurations of CONFIG3, for profiling:
+# the temporal stage (4000 frames, same lags) and the spatial stage (1024 x 1024 frames)
+CONFIG3_TALL = Scene(4000, 64, 64, 20, 1.5, 150.0, 1.0, 20.0, 0.05, "uint8", 0)
+CONFIG3_WIDE = Scene(64, 1024, 1024, 5000, 1.5, 150.0, 1.0, 20.0, 0.05, "uint8", 0)
 
 
 def _periodic_profile(pos: np.ndarray, n: int, sigma: float) -> np.ndarray:

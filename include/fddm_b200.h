@@ -79,7 +79,9 @@ int fddm_b200_workspace_size(int mode, int precision, uint64_t length, uint64_t 
      d_img_seq   (length, height, width) C-contiguous frames of `dtype`
      lags        HOST array of nlags lags in [0, length-1] (the reference's vector<unsigned>)
      nx, ny      padded FFT sizes (>= width, height; factors 2,3,5,7,11,13)
-     nt          temporal FFT length, >= 2*length-1 (factors 2,3,5,7,11,13)
+     nt          the reference's temporal FFT length; must be >= 2*length-1.  Any
+                 such length gives the same linear autocorrelation, so the library
+                 uses its own cheapest transform length >= 2*length-1
      d_window    (height, width) FP64 window or NULL (the reference's empty window)
      d_out       (nlags + 2, ny, nx/2 + 1) FP64 output: D(lag) rows in the order of
                  `lags`, then the power spectrum, then the variance; rows y-fftshifted
