@@ -13,8 +13,11 @@ constexpr int kMaxPass = 24;
 struct FftPlan {
   int n;                // transform length
   int npass;            // number of passes
+  int lgn;              // log2(n), or -1 when n is not a power of two
   int radix[kMaxPass];  // radix of pass s
   int block[kMaxPass];  // block size M_s at pass s (M_0 = n)
+  int lgstride[kMaxPass];  // log2(M_s / R_s) when a power of two, else -1
+  int lgbpf[kMaxPass];     // log2(n / R_s) when a power of two, else -1
 };
 
 struct SpatialArgs {

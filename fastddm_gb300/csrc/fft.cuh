@@ -152,17 +152,29 @@ template <class S> __host__ __device__ constexpr int swz_round(int n) {
 // offset f*ld of the (swizzled) buffer.
 // ---------------------------------------------------------------------------
 template <class S, int R, bool INV>
-__device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int ld, int n, int M,
-                                         const cx<S>* __restrict__ tw, int tid, int nthr) {
+__device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int ld, int n, int M, int lgs,
+                                         int lgb, const cx<S>* __restrict__ tw, int tid, int nthr) {
   const int stride = M / R;
   const int bpf = n / R;
   const int twstep = n / M;
   const int total = nfft * bpf;
   for (int beta = tid; beta < total; beta += nthr) {
-    const int f = beta / bpf;
-    const int loc = beta - f * bpf;
-    const int blk = loc / stride;
-    const int j = loc - blk * stride;
+    // power-of-two strides (the common case) index with shifts, others divide
+    int f, loc, blk, j;
+    if (lgb >= 0) {
+      f = beta >> lgb;
+      loc = beta & (bpf - 1);
+    } else {
+      f = beta / bpf;
+      loc = beta - f * bpf;
+    }
+    if (lgs >= 0) {
+      blk = loc >> lgs;
+      j = loc & (stride - 1);
+    } else {
+      blk = loc / stride;
+      j = loc - blk * stride;
+    }
     const int base = f * ld + blk * M + j;
     cx<S> v[R];
 #pragma unroll
@@ -186,17 +198,18 @@ __device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int 
 }
 
 template <class S, bool INV>
-__device__ __forceinline__ void fft_pass_dispatch(cx<S>* buf, int nfft, int ld, int n, int M, int R,
+__device__ __forceinline__ void fft_pass_dispatch(cx<S>* buf, int nfft, int ld, const FftPlan& p, int s,
                                                   const cx<S>* tw, int tid, int nthr) {
-  switch (R) {
-    case 2: fft_pass<S, 2, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
-    case 3: fft_pass<S, 3, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
-    case 4: fft_pass<S, 4, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
-    case 5: fft_pass<S, 5, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
-    case 7: fft_pass<S, 7, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
-    case 8: fft_pass<S, 8, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
-    case 11: fft_pass<S, 11, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
-    case 13: fft_pass<S, 13, INV>(buf, nfft, ld, n, M, tw, tid, nthr); break;
+  const int n = p.n, M = p.block[s], lgs = p.lgstride[s], lgb = p.lgbpf[s];
+  switch (p.radix[s]) {
+    case 2: fft_pass<S, 2, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
+    case 3: fft_pass<S, 3, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
+    case 4: fft_pass<S, 4, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
+    case 5: fft_pass<S, 5, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
+    case 7: fft_pass<S, 7, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
+    case 8: fft_pass<S, 8, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
+    case 11: fft_pass<S, 11, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
+    case 13: fft_pass<S, 13, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
     default: break;
   }
 }
@@ -207,7 +220,7 @@ template <class S>
 __device__ void fft_forward(cx<S>* buf, int nfft, int ld, const FftPlan& p, const cx<S>* tw, int tid,
                             int nthr) {
   for (int s = 0; s < p.npass; ++s) {
-    fft_pass_dispatch<S, false>(buf, nfft, ld, p.n, p.block[s], p.radix[s], tw, tid, nthr);
+    fft_pass_dispatch<S, false>(buf, nfft, ld, p, s, tw, tid, nthr);
     __syncthreads();
   }
 }
@@ -217,7 +230,7 @@ template <class S>
 __device__ void fft_inverse(cx<S>* buf, int nfft, int ld, const FftPlan& p, const cx<S>* tw, int tid,
                             int nthr) {
   for (int s = p.npass - 1; s >= 0; --s) {
-    fft_pass_dispatch<S, true>(buf, nfft, ld, p.n, p.block[s], p.radix[s], tw, tid, nthr);
+    fft_pass_dispatch<S, true>(buf, nfft, ld, p, s, tw, tid, nthr);
     __syncthreads();
   }
 }

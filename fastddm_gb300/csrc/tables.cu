@@ -27,9 +27,18 @@ bool make_plan(int n, FftPlan& p) {
   for (int r : odd)
     while (m % r == 0) if (!push(r)) return false;
   if (m != 1) return false;
+  auto lg = [](int v) -> int {
+    if (v <= 0 || (v & (v - 1))) return -1;
+    int l = 0;
+    while ((1 << l) < v) ++l;
+    return l;
+  };
+  p.lgn = lg(n);
   int M = n;
   for (int s = 0; s < p.npass; ++s) {
     p.block[s] = M;
+    p.lgstride[s] = lg(M / p.radix[s]);
+    p.lgbpf[s] = lg(n / p.radix[s]);
     M /= p.radix[s];
   }
   return true;
