@@ -71,11 +71,38 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   unsigned char* ws = static_cast<unsigned char*>(r.work);
 
   FftTables tx, ty, tt, tt2;
-  if (!get_tables(nx, kind, tx, err) || !get_tables(ny, kind, ty, err)) return 3;
   const int N = L.nt_fft;
-  if (r.mode == MODE_FFT && (!get_tables(N, kind, tt, err) || !get_tables(N / 2, kind, tt2, err))) return 3;
-
   cudaError_t ce;
+  if (!r.inline_tables) {
+    if (!get_tables(nx, kind, tx, err) || !get_tables(ny, kind, ty, err)) return 3;
+    if (r.mode == MODE_FFT && (!get_tables(N, kind, tt, err) || !get_tables(N / 2, kind, tt2, err))) return 3;
+  } else {
+    // copy host-computed tables into the workspace (no device allocation)
+    unsigned char* tp = ws + L.tables_off;
+    auto upload = [&](int n, FftTables& t) -> bool {
+      const HostTables* h = nullptr;
+      if (!host_tables(n, kind, h, err)) return false;
+      auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+      unsigned char* twp = tp;
+      int* pp = reinterpret_cast<int*>(tp + up(h->tw.size()));
+      int* ip = reinterpret_cast<int*>(tp + up(h->tw.size()) + up(sizeof(int) * (size_t)n));
+      if ((ce = cudaMemcpyAsync(twp, h->tw.data(), h->tw.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+          (ce = cudaMemcpyAsync(pp, h->perm.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+          (ce = cudaMemcpyAsync(ip, h->iperm.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+        err = cudaGetErrorString(ce);
+        return false;
+      }
+      t.plan = h->plan;
+      t.tw = twp;
+      t.perm = pp;
+      t.iperm = ip;
+      tp += inline_table_bytes(n, kind);
+      return true;
+    };
+    if (!upload(nx, tx) || !upload(ny, ty)) return 3;
+    if (r.mode == MODE_FFT && (!upload(N, tt) || !upload(N / 2, tt2))) return 3;
+  }
+
   // window in the FFT scalar type
   const void* win_s = nullptr;
   if (r.window) {
@@ -111,7 +138,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     }
   }
 
-  StageEvents* evs = stage_events();
+  StageEvents* evs = r.inline_tables ? nullptr : stage_events();
   if (evs) cudaEventRecord(evs->ev[0], st);
   int launches = r.window ? 1 : 0;
 

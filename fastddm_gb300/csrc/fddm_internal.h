@@ -65,17 +65,22 @@ enum Mode { MODE_FFT = 0, MODE_DIFF = 1 };
 enum DType { DT_U8 = 0, DT_I16 = 1, DT_U16 = 2, DT_I32 = 3, DT_U32 = 4, DT_I64 = 5, DT_U64 = 6, DT_F32 = 7, DT_F64 = 8 };
 
 struct DdmRequest {
-  int mode;
-  int precision;
-  const void* img;
-  int dtype;
-  int64_t T, H, W;
+  int mode = 0;
+  int precision = 0;
+  const void* img = nullptr;
+  int dtype = 0;
+  int64_t T = 0, H = 0, W = 0;
   std::vector<int> lags;
-  int64_t nx, ny, nt;
-  const double* window;  // device (H, W) or null
-  double* out;           // device (nlags + 2, ny, nx/2 + 1)
-  void* work;
-  size_t work_bytes;
+  int64_t nx = 0, ny = 0, nt = 0;
+  const double* window = nullptr;  // device (H, W) or null
+  double* out = nullptr;           // device (nlags + 2, ny, nx/2 + 1)
+  void* work = nullptr;
+  size_t work_bytes = 0;
+  // Workspace-only mode: FFT tables are copied into the workspace on every
+  // call instead of coming from the per-device cache (which allocates on
+  // first use), and the frame chunk shrinks until the layout fits max_work.
+  bool inline_tables = false;
+  size_t max_work = 0;  // 0: no limit
 };
 
 struct WorkLayout {
@@ -83,6 +88,7 @@ struct WorkLayout {
   size_t rbuf_off, rbuf_bytes;
   size_t win_off, win_bytes;
   size_t lags_off, rcp_off, slot_off, need_off;
+  size_t tables_off, tables_bytes;  // inline FFT tables (DdmRequest::inline_tables)
   size_t total;
   int Tpad, Hpad, chunk, pairs_per_block, cols_per_block, frames_per_block;
   int nt_fft;  // temporal transform length actually used (fft mode)
@@ -133,5 +139,16 @@ struct FftTables {
 };
 // kind: 0 = ff (16 B twiddles), 1 = double, 2 = float
 bool get_tables(int n, int kind, FftTables& out, std::string& err);
+
+// Host copy of the same tables (cached, never freed), for uploading into a
+// caller-provided workspace.
+struct HostTables {
+  FftPlan plan;
+  std::vector<unsigned char> tw;
+  std::vector<int> perm, iperm;
+};
+bool host_tables(int n, int kind, const HostTables*& out, std::string& err);
+// Bytes one transform's tables take inside a workspace (256-byte aligned parts).
+size_t inline_table_bytes(int n, int kind);
 
 }  // namespace fddm

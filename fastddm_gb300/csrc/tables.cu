@@ -64,8 +64,60 @@ struct Entry {
 };
 std::mutex g_mu;
 std::map<std::tuple<int, int, int>, Entry> g_cache;  // (device, n, kind)
+std::mutex g_host_mu;
+std::map<std::pair<int, int>, HostTables> g_host_cache;  // (n, kind)
 const long double kPi = 3.141592653589793238462643383279502884L;
+
+// Plan, permutations and twiddles w_n^k = exp(-2 pi i k / n) (extended precision).
+bool build_tables(int n, int kind, FftPlan& plan, std::vector<unsigned char>& tw, std::vector<int>& perm,
+                  std::vector<int>& iperm, std::string& err) {
+  if (!make_plan(n, plan)) {
+    err = "length " + std::to_string(n) + " has a prime factor other than 2, 3, 5, 7, 11, 13";
+    return false;
+  }
+  perm.assign(n, 0);
+  iperm.assign(n, 0);
+  for (int k = 0; k < n; ++k) perm[k] = perm_of(plan, k);
+  for (int k = 0; k < n; ++k) iperm[perm[k]] = k;
+  const size_t esz = kind == 2 ? 8 : 16;
+  tw.assign(esz * (size_t)n, 0);
+  for (int k = 0; k < n; ++k) {
+    const long double ang = -2.0L * kPi * (long double)k / (long double)n;
+    const long double c = cosl(ang), s = sinl(ang);
+    if (kind == 0) {
+      float v[4];
+      v[0] = (float)c; v[1] = (float)(c - (long double)v[0]);
+      v[2] = (float)s; v[3] = (float)(s - (long double)v[2]);
+      memcpy(&tw[esz * k], v, sizeof(v));
+    } else if (kind == 1) {
+      double v[2] = {(double)c, (double)s};
+      memcpy(&tw[esz * k], v, sizeof(v));
+    } else {
+      float v[2] = {(float)c, (float)s};
+      memcpy(&tw[esz * k], v, sizeof(v));
+    }
+  }
+  return true;
+}
 }  // namespace
+
+bool host_tables(int n, int kind, const HostTables*& out, std::string& err) {
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  auto key = std::make_pair(n, kind);
+  auto it = g_host_cache.find(key);
+  if (it == g_host_cache.end()) {
+    HostTables h;
+    if (!build_tables(n, kind, h.plan, h.tw, h.perm, h.iperm, err)) return false;
+    it = g_host_cache.emplace(key, std::move(h)).first;
+  }
+  out = &it->second;
+  return true;
+}
+
+size_t inline_table_bytes(int n, int kind) {
+  auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+  return up((size_t)n * (kind == 2 ? 8 : 16)) + 2 * up((size_t)n * sizeof(int));
+}
 
 bool get_tables(int n, int kind, FftTables& out, std::string& err) {
   int dev = 0;
@@ -76,32 +128,9 @@ bool get_tables(int n, int kind, FftTables& out, std::string& err) {
   auto it = g_cache.find(key);
   if (it == g_cache.end()) {
     Entry e;
-    if (!make_plan(n, e.plan)) {
-      err = "length " + std::to_string(n) + " has a prime factor other than 2, 3, 5, 7, 11, 13";
-      return false;
-    }
-    std::vector<int> perm(n), iperm(n);
-    for (int k = 0; k < n; ++k) perm[k] = perm_of(e.plan, k);
-    for (int k = 0; k < n; ++k) iperm[perm[k]] = k;
-    const size_t esz = kind == 2 ? 8 : 16;
-    std::vector<unsigned char> tw(esz * (size_t)n);
-    for (int k = 0; k < n; ++k) {
-      // w_n^k = exp(-2 pi i k / n) in extended precision
-      const long double ang = -2.0L * kPi * (long double)k / (long double)n;
-      const long double c = cosl(ang), s = sinl(ang);
-      if (kind == 0) {
-        float v[4];
-        v[0] = (float)c; v[1] = (float)(c - (long double)v[0]);
-        v[2] = (float)s; v[3] = (float)(s - (long double)v[2]);
-        memcpy(&tw[esz * k], v, sizeof(v));
-      } else if (kind == 1) {
-        double v[2] = {(double)c, (double)s};
-        memcpy(&tw[esz * k], v, sizeof(v));
-      } else {
-        float v[2] = {(float)c, (float)s};
-        memcpy(&tw[esz * k], v, sizeof(v));
-      }
-    }
+    std::vector<unsigned char> tw;
+    std::vector<int> perm, iperm;
+    if (!build_tables(n, kind, e.plan, tw, perm, iperm, err)) return false;
     if ((ce = cudaMalloc(&e.tw, tw.size())) != cudaSuccess ||
         (ce = cudaMalloc(reinterpret_cast<void**>(&e.perm), sizeof(int) * n)) != cudaSuccess ||
         (ce = cudaMalloc(reinterpret_cast<void**>(&e.iperm), sizeof(int) * n)) != cudaSuccess ||
@@ -232,7 +261,33 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
   L.slot_off = off; off = align_up(off + 2 * (size_t)(r.T + 1) * sizeof(int), 256);
   L.need_off = off;
   if (r.mode == MODE_FFT) off = align_up(off + (size_t)kMaxTemporalCtas * (2 * r.lags.size() + 2) * ea, 256);
+  L.tables_off = off;
+  L.tables_bytes = 0;
+  if (r.inline_tables) {
+    const int kind = r.precision == PREC_FF ? 0 : r.precision == PREC_F64 ? 1 : 2;
+    L.tables_bytes = inline_table_bytes((int)r.nx, kind) + inline_table_bytes((int)r.ny, kind);
+    if (r.mode == MODE_FFT) L.tables_bytes += inline_table_bytes(L.nt_fft, kind) + inline_table_bytes(L.nt_fft / 2, kind);
+    off += L.tables_bytes;
+  }
   L.total = off;
+  if (r.max_work > 0 && L.total > r.max_work) {
+    // a smaller frame chunk is the only part that can shrink
+    const size_t fixed = L.total - align_up(L.rbuf_bytes, 256);
+    const size_t room = r.max_work > fixed ? r.max_work - fixed : 0;
+    int c = (int)std::min<size_t>((size_t)L.chunk, room / std::max<size_t>(per_frame, 1));
+    c = c / L.frames_per_block * L.frames_per_block;
+    if (c < L.frames_per_block) {
+      err = "needs " + std::to_string(fixed + (size_t)L.frames_per_block * per_frame) +
+            " bytes of workspace, more than the " + std::to_string(r.max_work) + " available";
+      return false;
+    }
+    const size_t shrink = align_up(L.rbuf_bytes, 256) - align_up((size_t)c * per_frame, 256);
+    L.chunk = c;
+    L.rbuf_bytes = (size_t)c * per_frame;
+    L.win_off -= shrink; L.lags_off -= shrink; L.rcp_off -= shrink; L.slot_off -= shrink;
+    L.need_off -= shrink; L.tables_off -= shrink;
+    L.total -= shrink;
+  }
   return true;
 }
 

@@ -124,6 +124,22 @@ int fddm_b200_azimuthal_average(const double* d_data, uint64_t nrows, uint64_t n
                                 const double* d_weight, const double* d_sumw, const double* d_bias,
                                 double* d_avg, double* d_err, void* stream);
 
+/* Image structure function, fft mode, without any device allocation.
+   This entry point has no counterpart in the reference.  It is for callers
+   that cannot call cudaMalloc when they need a result (an acquisition callback
+   that must not wait on the allocator, a plugin whose host owns all device
+   memory): the caller passes the frames, the window and the output only, and
+   the library calls no cudaMalloc, cudaFree or allocating routine.  Its scratch
+   is one 64 MiB array in device memory that every device loading the library
+   holds until the process exits; a problem needing more is rejected with
+   FDDM_ERR_NOMEM.  All calls share that array, so calls that overlap on the GPU
+   race and must be serialised by the caller.  The first call on a device looks
+   up the array's device address with that device current; make it before any
+   stream capture.  Arguments and result as fddm_b200_ddm_fft. */
+int fddm_b200_ddm_fft_noalloc(const void* d_img_seq, int dtype, uint64_t length, uint64_t height, uint64_t width,
+                              const uint32_t* lags, uint64_t nlags, uint64_t nx, uint64_t ny, uint64_t nt,
+                              const double* d_window, double* d_out, int precision, void* stream);
+
 /* Diagnostics (no counterpart in the reference, which has no tracing).
    fddm_b200_set_stage_timing(1) makes every following ddm call record CUDA
    events on its stream around the spatial stage (row and column FFT passes)
