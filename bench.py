@@ -75,14 +75,20 @@ def _cpu_spatial(args):
 
 
 def _cpu_temporal(args):
+    """Temporal stage of the oracle on `nq` spectrum columns, in blocks of 2048 columns."""
     T, nq, lags, nt, seed = args
     sys.path.insert(0, str(ROOT / "oracle"))
     import ddm_oracle as oracle
 
     rng = np.random.default_rng(seed)
-    Fq = rng.standard_normal((T, nq)) + 1j * rng.standard_normal((T, nq))
+    blk = min(nq, 2048)
+    Fq = rng.standard_normal((T, blk)) + 1j * rng.standard_normal((T, blk))
     t0 = time.perf_counter()
-    oracle.temporal_fft(Fq, lags, nt)
+    done = 0
+    while done < nq:
+        n = min(blk, nq - done)
+        oracle.temporal_fft(Fq[:, :n], lags, nt)
+        done += n
     return time.perf_counter() - t0, nq
 
 
@@ -200,14 +206,14 @@ def run_reference(args):
     T, H, W = scene.length, scene.height, scene.width
     nx, ny, nt = next_fast_len(W, "cpp"), next_fast_len(H, "cpp"), next_fast_len(2 * T, "cpp")
     Q = ny * (nx // 2 + 1)
-    small = synthetic.Scene(4, H, W, max(1, scene.n_spots), scene.sigma, scene.amplitude, scene.diffusivity,
+    small = synthetic.Scene(16, H, W, max(1, scene.n_spots), scene.sigma, scene.amplitude, scene.diffusivity,
                             scene.offset, scene.drift, scene.dtype, scene.seed)
     frames = synthetic.make_stack(small)
     workers = os.cpu_count() or 1
     values = []
     with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as pool:
         for i in range(args.warmup + args.steps):
-            v, _ = cpu_throughput(frames, T, Q, nx, ny, nt, lags, workers, 2, 64, pool)
+            v, _ = cpu_throughput(frames, T, Q, nx, ny, nt, lags, workers, 4, 2048, pool)
             if i >= args.warmup:
                 values.append(v)
     value = statistics.mean(values)
@@ -217,7 +223,7 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_desc(args.config, scene, lags, "f64", "fft"),
         "cpu_baseline": {"value": value, "unit": "frames/s", "cores": workers, "kind": "port",
-                         "sample": f"per step and worker: spatial FFT of 2 frames and the temporal stage of 64 "
+                         "sample": f"per step and worker: spatial FFT of 4 frames and the temporal stage of 2048 "
                                    f"q-columns x {T} frames; full-job time extrapolated as T/spatial_rate + "
                                    f"Q/temporal_rate (numpy FP64 restatement of the cpp core; the cpp core itself "
                                    f"needs FFTW's CMake build)"},
@@ -357,10 +363,10 @@ def run_ours(args):
 
     cpu = None
     if not args.no_cpu and rank == 0 and ws == 1:
-        sample = frames[:2].cpu().numpy()
-        v, wall = cpu_throughput(sample, T, Q, nx, ny, nt, lags, 1, 2, 256, None)
+        sample = frames[:32].cpu().numpy()
+        v, wall = cpu_throughput(sample, T, Q, nx, ny, nt, lags, 1, 32, 16384, None)
         cpu = {"value": v, "unit": "frames/s", "cores": 1, "kind": "port",
-               "sample": f"spatial FFT of 2 frames and the temporal stage of 256 q-columns x {T} frames "
+               "sample": f"spatial FFT of 32 frames and the temporal stage of 16384 q-columns x {T} frames "
                          f"(FP64 numpy restatement of the cpp core), extrapolated to the full job; {wall:.1f} s"}
 
     if rank == 0:
@@ -376,6 +382,72 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_validate(args):
+    """Max relative error of the b200 result on a sample of Fourier modes of the full workload.
+
+    The reference values come from direct FP64 DFTs of every frame at the
+    sampled modes (8 kx columns including kx = 0, all ky) and the direct
+    difference formula for D (no Wiener-Khinchin cancellation), PS and VAR.
+    """
+    import torch
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import ddm_oracle as oracle
+    from fastddm_gb300 import synthetic, window as fwin
+    from fastddm_gb300._ddm_b200 import DdmPlan
+    from fastddm_gb300._fftopt import next_fast_len
+
+    device = torch.device("cuda", 0)
+    scene = getattr(synthetic, CONFIGS[args.config])
+    lags = lags_for(args.config, scene.length)
+    T, H, W = scene.length, scene.height, scene.width
+    nx, ny, nt = next_fast_len(W, "b200"), next_fast_len(H, "b200"), next_fast_len(2 * T, "b200")
+    nkx = nx // 2 + 1
+    frames = synthetic.make_stack_torch(scene, device=device)
+    code = {torch.uint8: 0, torch.int16: 1}.get(frames.dtype, 2)
+    wnp = fwin.blackman_harris((H, W)) if args.config == "medium" else None
+    window = torch.from_numpy(wnp).to(device) if wnp is not None else None
+    results = {}
+    outs = {}
+    for mode, prec in (("fft", args.precision), ("diff", args.precision), ("fft", "f64")):
+        plan = DdmPlan(mode, T, H, W, code, lags, nx, ny, nt if mode == "fft" else 0, window is not None, prec, device)
+        out = torch.empty(plan.out_shape, dtype=torch.float64, device=device)
+        plan.run(frames, window, out)
+        torch.cuda.synchronize()
+        outs[(mode, prec)] = out.cpu().numpy()
+        del plan, out
+        torch.cuda.empty_cache()
+    # sampled exact spectra: columns kx in `cols`, every ky
+    cols = sorted({0, 1, 2, 5, 17, nkx // 4, nkx // 2, nkx - 1})
+    ex = np.exp(-2j * np.pi * np.outer(np.arange(W), np.array(cols)) / nx)          # (W, C)
+    ey = np.exp(-2j * np.pi * np.outer(np.fft.fftfreq(ny) * ny, np.arange(H)) / ny)  # (ny, H)
+    Fs = np.empty((T, ny, len(cols)), dtype=np.complex128)
+    host = frames.cpu().numpy()
+    for t0 in range(0, T, 64):
+        blk = host[t0:t0 + 64].astype(np.float64)
+        if wnp is not None:
+            blk = blk * wnp
+        Fs[t0:t0 + 64] = (ey @ (blk @ ex)) / math.sqrt(nx * ny)
+    Fq = Fs.reshape(T, -1)
+    exact = oracle.temporal_diff(Fq, lags)  # D by differences; VAR recomputed below without cancellation
+    G = Fq - Fq.mean(axis=0)
+    exact[-1] = (G.real ** 2 + G.imag ** 2).mean(axis=0)
+    exact = exact.reshape(len(lags) + 2, ny, len(cols))
+    exact = np.fft.fftshift(exact, axes=1)
+    for key, out in outs.items():
+        got = out[:, :, cols]
+        e = np.abs(got - exact) / np.abs(exact)
+        e_nodc = e.copy()
+        e_nodc[:, ny // 2, cols.index(0)] = 0
+        results[f"{key[0]}_{key[1]}"] = {"max_rel": float(e.max()), "max_rel_noDC": float(e_nodc.max()),
+                                         "median_rel": float(np.median(e))}
+    a, b = outs[("fft", args.precision)], outs[("diff", args.precision)]
+    results["fft_vs_diff_all_modes"] = float(np.max(np.abs(a - b) / np.abs(b)))
+    results["fft_vs_f64_all_modes"] = float(np.max(np.abs(a - outs[("fft", "f64")]) / np.abs(outs[("fft", "f64")])))
+    print(json.dumps({"validate": args.config, "sampled_modes": len(cols) * ny, "kx_columns": cols,
+                      "lags": int(len(lags)), "errors": results}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -387,8 +459,11 @@ def main():
     ap.add_argument("--precision", default="ff", choices=["ff", "f64", "f32"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--validate", action="store_true", help="report sampled errors against exact FP64 spectra")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.validate:
+        run_validate(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
