@@ -20,7 +20,7 @@ from typing import Callable, Dict, Iterable, Optional
 import numpy as np
 
 from ._config import DTYPE
-from ._ddm_b200 import ddm_device, ddm_diff_b200, ddm_fft_b200, to_host
+from ._ddm_b200 import ddm_device, ddm_diff_b200, ddm_fft_b200
 from ._fftopt import next_fast_len
 from .imagestructurefunction import ImageStructureFunction
 
@@ -81,8 +81,8 @@ def ddm(
     ky = 2 * np.pi * np.fft.fftshift(np.fft.fftfreq(ny))
 
     if core == "b200" and keep_on_device:
-        dev = ddm_device(img_seq, lags, nx, ny, nt, window, mode=mode, **kwargs)
-        data = to_host(dev)
+        dev, host = ddm_device(img_seq, lags, nx, ny, nt, window, mode=mode, host_out=True, **kwargs)
+        data = host.numpy()
     else:
         func = backend[core][mode]
         args = [img_seq, lags, nx, ny] + ([nt] if mode == "fft" else []) + [window.astype(DTYPE)]

@@ -73,6 +73,22 @@ def frames_to_device(img_seq, device) -> tuple["torch.Tensor", int]:
             raise TypeError(f"unsupported image dtype {t.dtype}")
         t = t.to(device).contiguous()
         return t, _TORCH_CODE[t.dtype]
+    arr, code = host_frames(img_seq)
+    raw = torch.from_numpy(arr.reshape(-1).view(np.uint8))
+    dev = torch.empty(raw.numel(), dtype=torch.uint8, device=device)
+    dev.copy_(raw)
+    return dev, code
+
+
+def host_frames(img_seq):
+    """Host image sequence as a C-contiguous array (or CPU tensor) the library can read; returns (array, code)."""
+    if torch is not None and isinstance(img_seq, torch.Tensor):
+        t = img_seq
+        if t.dtype == torch.int64 or (hasattr(torch, "uint64") and t.dtype == torch.uint64):
+            t = t.to(torch.float64)
+        if t.dtype not in _TORCH_CODE:
+            raise TypeError(f"unsupported image dtype {t.dtype}")
+        return t.contiguous(), _TORCH_CODE[t.dtype]
     arr = np.asarray(img_seq)
     if arr.ndim != 3:
         raise ValueError("img_seq must have shape (t, y, x)")
@@ -81,11 +97,15 @@ def frames_to_device(img_seq, device) -> tuple["torch.Tensor", int]:
     code = _lib.DTYPE_CODE.get(arr.dtype.name)
     if code is None or code in (5, 6):
         raise TypeError(f"unsupported image dtype {arr.dtype}")
-    arr = np.ascontiguousarray(arr)
-    raw = torch.from_numpy(arr.reshape(-1).view(np.uint8))
-    dev = torch.empty(raw.numel(), dtype=torch.uint8, device=device)
-    dev.copy_(raw)
-    return dev, code
+    return np.ascontiguousarray(arr), code
+
+
+def _host_ptr(a) -> int:
+    return a.data_ptr() if (torch is not None and isinstance(a, torch.Tensor)) else a.ctypes.data
+
+
+def _host_nbytes(a) -> int:
+    return a.numel() * a.element_size() if (torch is not None and isinstance(a, torch.Tensor)) else a.nbytes
 
 
 @dataclass
@@ -166,6 +186,31 @@ class DdmPlan:
         _lib.check(code)
         return out
 
+    def run_from_host(self, host, frames_dev: "torch.Tensor", window: Optional["torch.Tensor"], out: "torch.Tensor",
+                      host_out: Optional["torch.Tensor"] = None,
+                      stream: Optional["torch.cuda.Stream"] = None) -> "torch.Tensor":
+        """Enqueue the computation reading the frames from host memory (upload overlapped with compute).
+
+        `host` must stay alive until the stream has finished; `host_out`, if
+        given, receives the result (page-locked memory makes the copy async).
+        """
+        lib = _lib.load()
+        if stream is None:
+            stream = torch.cuda.current_stream(self.device)
+        if out.dtype != torch.float64 or tuple(out.shape) != self.out_shape or not out.is_contiguous():
+            raise ValueError(f"out must be a contiguous float64 tensor of shape {self.out_shape}")
+        lags_p = self._lags_c.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        wptr = window.data_ptr() if window is not None else None
+        hout = host_out.data_ptr() if host_out is not None else None
+        with torch.cuda.device(self.device):
+            code = lib.fddm_b200_ddm_from_host(
+                _lib.MODE[self.mode], _host_ptr(host), self.dtype_code, self.length, self.height, self.width,
+                lags_p, len(self._lags_c), self.nx, self.ny, self.nt, frames_dev.data_ptr(), wptr, out.data_ptr(),
+                hout, self.workspace.data_ptr(), self.workspace_bytes, _lib.PREC[self.precision], stream.cuda_stream,
+            )
+        _lib.check(code)
+        return out
+
 
 def _window_to_device(window, device) -> Optional["torch.Tensor"]:
     if window is None:
@@ -181,21 +226,41 @@ def _window_to_device(window, device) -> Optional["torch.Tensor"]:
 
 
 def ddm_device(img_seq, lags: Sequence[int], nx: int, ny: int, nt: int, window=None, *, mode: str = "fft",
-               precision: str = "ff", gpu_id: int = 0) -> "torch.Tensor":
-    """Run the structure function and return the device-resident result tensor."""
+               precision: str = "ff", gpu_id: int = 0, host_out: bool = False):
+    """Run the structure function; returns the device result tensor (and the host copy if `host_out`).
+
+    Device-resident input (a CUDA tensor) is used in place; host input (numpy
+    or a CPU tensor) is uploaded in chunks overlapped with the spatial FFTs.
+    """
     _require_torch()
     device = _device(gpu_id)
-    frames, code = frames_to_device(img_seq, device)
     shape = tuple(img_seq.shape)
     if len(shape) != 3:
         raise ValueError("img_seq must have shape (t, y, x)")
     wdev = _window_to_device(window, device)
     if wdev is not None and tuple(wdev.shape) != shape[1:]:
         raise RuntimeError(f"Window with shape {tuple(wdev.shape)} incompatible with image shape {shape[1:]}.")
+    on_device = torch is not None and isinstance(img_seq, torch.Tensor) and img_seq.is_cuda
+    if on_device:
+        frames, code = frames_to_device(img_seq, device)
+    else:
+        host, code = host_frames(img_seq)
     plan = DdmPlan(mode, shape[0], shape[1], shape[2], code, np.asarray(lags), int(nx), int(ny),
                    int(nt) if mode == "fft" else 0, wdev is not None, precision, device)
     out = torch.empty(plan.out_shape, dtype=torch.float64, device=device)
-    plan.run(frames, wdev, out)
+    hout = torch.empty(plan.out_shape, dtype=torch.float64, pin_memory=True) if host_out else None
+    stream = torch.cuda.current_stream(device)
+    if on_device:
+        plan.run(frames, wdev, out, stream)
+        if hout is not None:
+            hout.copy_(out, non_blocking=True)
+    else:
+        staging = torch.empty(_host_nbytes(host), dtype=torch.uint8, device=device)
+        plan.run_from_host(host, staging, wdev, out, hout, stream)
+    if hout is not None:
+        stream.synchronize()  # the host arrays must outlive the queued copies
+        return out, hout
+    stream.synchronize()
     return out
 
 
@@ -208,11 +273,13 @@ def to_host(out: "torch.Tensor") -> np.ndarray:
 
 def ddm_fft_b200(img_seq, lags, nx, ny, nt, window, *, gpu_id: int = 0, precision: str = "ff", **kwargs) -> np.ndarray:
     """Image structure function, fft mode (Wiener-Khinchin), on the GB300."""
-    out = ddm_device(img_seq, lags, nx, ny, nt, window, mode="fft", precision=precision, gpu_id=gpu_id)
-    return to_host(out)
+    _, hout = ddm_device(img_seq, lags, nx, ny, nt, window, mode="fft", precision=precision, gpu_id=gpu_id,
+                         host_out=True)
+    return hout.numpy()
 
 
 def ddm_diff_b200(img_seq, lags, nx, ny, window, *, gpu_id: int = 0, precision: str = "ff", **kwargs) -> np.ndarray:
     """Image structure function, diff mode (direct differences), on the GB300."""
-    out = ddm_device(img_seq, lags, nx, ny, 0, window, mode="diff", precision=precision, gpu_id=gpu_id)
-    return to_host(out)
+    _, hout = ddm_device(img_seq, lags, nx, ny, 0, window, mode="diff", precision=precision, gpu_id=gpu_id,
+                         host_out=True)
+    return hout.numpy()

@@ -55,6 +55,11 @@ _SIGNATURES = {
         [_vp, ctypes.c_int, _u64, _u64, _u64, ctypes.POINTER(ctypes.c_uint32), _u64, _u64, _u64,
          _vp, _vp, _vp, ctypes.c_size_t, ctypes.c_int, _vp],
     ),
+    "fddm_b200_ddm_from_host": (
+        ctypes.c_int,
+        [ctypes.c_int, _vp, ctypes.c_int, _u64, _u64, _u64, ctypes.POINTER(ctypes.c_uint32), _u64, _u64, _u64,
+         _u64, _vp, _vp, _vp, _vp, _vp, ctypes.c_size_t, ctypes.c_int, _vp],
+    ),
     "fddm_b200_ddm_fft_noalloc": (
         ctypes.c_int,
         [_vp, ctypes.c_int, _u64, _u64, _u64, ctypes.POINTER(ctypes.c_uint32), _u64, _u64, _u64, _u64,

@@ -31,10 +31,13 @@ bool map_dtype(int dtype, int& out) {
 
 int run(int mode, const void* img, int dtype, uint64_t length, uint64_t height, uint64_t width,
         const uint32_t* lags, uint64_t nlags, uint64_t nx, uint64_t ny, uint64_t nt, const double* window,
-        double* out, void* work, size_t work_bytes, int precision, void* stream) {
+        double* out, void* work, size_t work_bytes, int precision, void* stream,
+        const void* host_img = nullptr, double* host_out = nullptr) {
   g_last_error.clear();
   if (!img || !out || (nlags && !lags) || !work) return fail(FDDM_ERR_INVALID, "null pointer argument");
   fddm::DdmRequest r;
+  r.host_img = host_img;
+  r.host_out = host_out;
   r.mode = mode;
   r.precision = precision;
   if (precision != FDDM_PREC_FF && precision != FDDM_PREC_F64 && precision != FDDM_PREC_F32)
@@ -70,6 +73,39 @@ std::map<int, StageEvents> g_events;  // per device
 }  // namespace
 
 void count_launches(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+namespace {
+std::mutex g_copy_mu;
+std::map<int, CopyCtx> g_copy;  // per device
+}  // namespace
+
+CopyCtx* copy_ctx(std::string& err) {
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return nullptr; }
+  std::lock_guard<std::mutex> lk(g_copy_mu);
+  auto it = g_copy.find(dev);
+  if (it == g_copy.end()) {
+    CopyCtx c{};
+    if ((ce = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (ce = cudaEventCreateWithFlags(&c.ready, cudaEventDisableTiming)) != cudaSuccess ||
+        (ce = cudaEventCreateWithFlags(&c.start, cudaEventDisableTiming)) != cudaSuccess) {
+      err = cudaGetErrorString(ce);
+      return nullptr;
+    }
+    it = g_copy.emplace(dev, c).first;
+  }
+  return &it->second;
+}
+
+size_t dtype_bytes(int dtype) {
+  switch (dtype) {
+    case DT_U8: return 1;
+    case DT_I16: case DT_U16: return 2;
+    case DT_I32: case DT_U32: case DT_F32: return 4;
+    default: return 8;
+  }
+}
 
 StageEvents* stage_events() {
   if (!g_timing.load()) return nullptr;
@@ -153,5 +189,16 @@ int fddm_b200_stage_times(float* spatial_ms, float* temporal_ms) {
 }
 
 uint64_t fddm_b200_launch_count(void) { return fddm::g_launches.load(); }
+
+int fddm_b200_ddm_from_host(int mode, const void* h_img_seq, int dtype, uint64_t length, uint64_t height,
+                            uint64_t width, const uint32_t* lags, uint64_t nlags, uint64_t nx, uint64_t ny,
+                            uint64_t nt, void* d_frames, const double* d_window, double* d_out, double* h_out,
+                            void* d_workspace, size_t workspace_bytes, int precision, void* stream) {
+  if (!h_img_seq) return fail(FDDM_ERR_INVALID, "null pointer argument");
+  if (mode != FDDM_MODE_FFT && mode != FDDM_MODE_DIFF) return fail(FDDM_ERR_INVALID, "unknown mode");
+  return run(mode == FDDM_MODE_FFT ? fddm::MODE_FFT : fddm::MODE_DIFF, d_frames, dtype, length, height, width, lags,
+             nlags, nx, ny, mode == FDDM_MODE_FFT ? nt : 0, d_window, d_out, d_workspace, workspace_bytes, precision,
+             stream, h_img_seq, h_out);
+}
 
 }  // extern "C"

@@ -162,9 +162,30 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   const size_t smem_rows = (size_t)swz_round<S>(L.pairs_per_block * nx) * sizeof(cx<S>);
   const size_t smem_cols = (size_t)swz_round<S>(L.cols_per_block * L.frames_per_block * ny) * sizeof(cx<S>);
   if ((ce = allow_smem(k_cols<S>, smem_cols)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+  CopyCtx* cp = nullptr;
+  const size_t frame_bytes = (size_t)H * W * dtype_bytes(r.dtype);
+  if (r.host_img) {
+    if (!(cp = copy_ctx(err))) return 3;
+    // the copies may only overwrite the frame buffer after earlier work on `st`
+    if ((ce = cudaEventRecord(cp->start, st)) != cudaSuccess || (ce = cudaStreamWaitEvent(cp->stream, cp->start, 0)) != cudaSuccess) {
+      err = cudaGetErrorString(ce);
+      return 3;
+    }
+  }
   for (int t0 = 0; t0 < T; t0 += L.chunk) {
     sa.t0 = t0;
     sa.tc = std::min(L.chunk, T - t0);
+    if (r.host_img) {
+      const size_t off = (size_t)t0 * frame_bytes, n = (size_t)sa.tc * frame_bytes;
+      if ((ce = cudaMemcpyAsync(static_cast<unsigned char*>(const_cast<void*>(r.img)) + off,
+                                static_cast<const unsigned char*>(r.host_img) + off, n, cudaMemcpyHostToDevice,
+                                cp->stream)) != cudaSuccess ||
+          (ce = cudaEventRecord(cp->ready, cp->stream)) != cudaSuccess ||
+          (ce = cudaStreamWaitEvent(st, cp->ready, 0)) != cudaSuccess) {
+        err = cudaGetErrorString(ce);
+        return 3;
+      }
+    }
     dim3 gr((npairs + L.pairs_per_block - 1) / L.pairs_per_block, sa.tc);
     if ((ce = dispatch_rows<S>(r.dtype, sa, gr, smem_rows, st)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
     dim3 gc((nkx + L.cols_per_block - 1) / L.cols_per_block, (sa.tc + L.frames_per_block - 1) / L.frames_per_block);
@@ -211,6 +232,13 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
   if (evs) cudaEventRecord(evs->ev[2], st);
   count_launches(launches + 1);
+  if (r.host_out) {
+    const size_t bytes = (size_t)(nl + 2) * Q * sizeof(double);
+    if ((ce = cudaMemcpyAsync(r.host_out, r.out, bytes, cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
+      err = cudaGetErrorString(ce);
+      return 3;
+    }
+  }
   return 0;
 }
 

@@ -81,7 +81,20 @@ struct DdmRequest {
   // first use), and the frame chunk shrinks until the layout fits max_work.
   bool inline_tables = false;
   size_t max_work = 0;  // 0: no limit
+  // Host-resident input: frames are copied chunk by chunk from host_img into
+  // the device buffer `img` on a library copy stream, each chunk just before
+  // the spatial passes that read it; host_out (optional) receives the result.
+  const void* host_img = nullptr;
+  double* host_out = nullptr;
 };
+
+// Per-device copy stream and event used to overlap frame uploads with compute.
+struct CopyCtx {
+  cudaStream_t stream;
+  cudaEvent_t ready, start;
+};
+CopyCtx* copy_ctx(std::string& err);
+size_t dtype_bytes(int dtype);
 
 struct WorkLayout {
   size_t spec_off, spec_bytes;

@@ -42,22 +42,22 @@ template <class S> __device__ __forceinline__ S ksin(int idx) {
 // In-register DFTs of size R (forward: w = exp(-2 pi i / R); INV: conjugate).
 // ---------------------------------------------------------------------------
 template <class S, bool INV> __device__ __forceinline__ void dft2(cx<S>* v) {
-  cx<S> a = cadd(v[0], v[1]);
-  cx<S> b = csub(v[0], v[1]);
+  cx<S> a = badd(v[0], v[1]);
+  cx<S> b = bsub(v[0], v[1]);
   v[0] = a;
   v[1] = b;
 }
 
 template <class S, bool INV>
 __device__ __forceinline__ void dft4_vals(cx<S>& x0, cx<S>& x1, cx<S>& x2, cx<S>& x3) {
-  cx<S> t0 = cadd(x0, x2);
-  cx<S> t1 = csub(x0, x2);
-  cx<S> t2 = cadd(x1, x3);
-  cx<S> t3 = cmul_mi<S, INV>(csub(x1, x3));
-  x0 = cadd(t0, t2);
-  x2 = csub(t0, t2);
-  x1 = cadd(t1, t3);
-  x3 = csub(t1, t3);
+  cx<S> t0 = badd(x0, x2);
+  cx<S> t1 = bsub(x0, x2);
+  cx<S> t2 = badd(x1, x3);
+  cx<S> t3 = cmul_mi<S, INV>(bsub(x1, x3));
+  x0 = badd(t0, t2);
+  x2 = bsub(t0, t2);
+  x1 = badd(t1, t3);
+  x3 = bsub(t1, t3);
 }
 
 template <class S, bool INV> __device__ __forceinline__ void dft4(cx<S>* v) {
@@ -66,15 +66,15 @@ template <class S, bool INV> __device__ __forceinline__ void dft4(cx<S>* v) {
 
 template <class S, bool INV> __device__ __forceinline__ void dft8(cx<S>* v) {
   const S h = sc<S>::cst(kSqrtHalfH, kSqrtHalfL, kSqrtHalfD);
-  cx<S> a0 = cadd(v[0], v[4]), a1 = cadd(v[1], v[5]), a2 = cadd(v[2], v[6]), a3 = cadd(v[3], v[7]);
-  cx<S> b0 = csub(v[0], v[4]), b1 = csub(v[1], v[5]), b2 = csub(v[2], v[6]), b3 = csub(v[3], v[7]);
+  cx<S> a0 = badd(v[0], v[4]), a1 = badd(v[1], v[5]), a2 = badd(v[2], v[6]), a3 = badd(v[3], v[7]);
+  cx<S> b0 = bsub(v[0], v[4]), b1 = bsub(v[1], v[5]), b2 = bsub(v[2], v[6]), b3 = bsub(v[3], v[7]);
   // b_r *= w8^r  (forward w8 = (1 - i)/sqrt2, inverse its conjugate)
   if (!INV) {
-    b1 = cscale<S>({sc<S>::add(b1.r, b1.i), sc<S>::sub(b1.i, b1.r)}, h);
-    b3 = cscale<S>({sc<S>::sub(b3.i, b3.r), sc<S>::neg(sc<S>::add(b3.r, b3.i))}, h);
+    b1 = cscale<S>({bfly<S>::add(b1.r, b1.i), bfly<S>::sub(b1.i, b1.r)}, h);
+    b3 = cscale<S>({bfly<S>::sub(b3.i, b3.r), sc<S>::neg(bfly<S>::add(b3.r, b3.i))}, h);
   } else {
-    b1 = cscale<S>({sc<S>::sub(b1.r, b1.i), sc<S>::add(b1.r, b1.i)}, h);
-    b3 = cscale<S>({sc<S>::neg(sc<S>::add(b3.r, b3.i)), sc<S>::sub(b3.r, b3.i)}, h);
+    b1 = cscale<S>({bfly<S>::sub(b1.r, b1.i), bfly<S>::add(b1.r, b1.i)}, h);
+    b3 = cscale<S>({sc<S>::neg(bfly<S>::add(b3.r, b3.i)), bfly<S>::sub(b3.r, b3.i)}, h);
   }
   b2 = cmul_mi<S, INV>(b2);
   dft4_vals<S, INV>(a0, a1, a2, a3);
@@ -90,13 +90,13 @@ template <class S, int R, bool INV> __device__ __forceinline__ void dft_odd(cx<S
   cx<S> a[H], b[H];
 #pragma unroll
   for (int r = 1; r <= H; ++r) {
-    a[r - 1] = cadd(v[r], v[R - r]);
-    b[r - 1] = csub(v[r], v[R - r]);
+    a[r - 1] = badd(v[r], v[R - r]);
+    b[r - 1] = bsub(v[r], v[R - r]);
   }
   cx<S> x0 = v[0];
   cx<S> y0 = x0;
 #pragma unroll
-  for (int r = 0; r < H; ++r) y0 = cadd(y0, a[r]);
+  for (int r = 0; r < H; ++r) y0 = badd(y0, a[r]);
 #pragma unroll
   for (int m = 1; m <= H; ++m) {
     cx<S> re = x0;
@@ -106,17 +106,17 @@ template <class S, int R, bool INV> __device__ __forceinline__ void dft_odd(cx<S
       const int idx = OFF + (r * m) % R;
       const S c = kcos<S>(idx);
       const S s = ksin<S>(idx);
-      re = cadd(re, cscale(a[r - 1], c));
-      im = cadd(im, cscale(b[r - 1], s));
+      re = badd(re, cscale(a[r - 1], c));
+      im = badd(im, cscale(b[r - 1], s));
     }
     // forward: y_m = re - i*im, y_{R-m} = re + i*im
     cx<S> mi = cmul_mi<S, false>(im);  // -i * im
     if (!INV) {
-      v[m] = cadd(re, mi);
-      v[R - m] = csub(re, mi);
+      v[m] = badd(re, mi);
+      v[R - m] = bsub(re, mi);
     } else {
-      v[m] = csub(re, mi);
-      v[R - m] = cadd(re, mi);
+      v[m] = bsub(re, mi);
+      v[R - m] = badd(re, mi);
     }
   }
   v[0] = y0;

@@ -41,6 +41,16 @@ __device__ __forceinline__ ff ff_add(ff a, ff b) {
   return fast_two_sum(s.h, e);
 }
 __device__ __forceinline__ ff ff_neg(ff a) { return {-a.h, -a.l}; }
+
+// ff addition without the final renormalisation: the result (s, e) is exact
+// TwoSum of the high parts plus the rounded sum of the low parts, left as an
+// unevaluated pair.  Its absolute error is the same ~2^-47 (|a| + |b|); only the
+// split between the two words is not canonical.  Used inside FFT butterflies,
+// whose twiddle products renormalise (ff_dot2 ends with a fast TwoSum).
+__device__ __forceinline__ ff ff_add_nn(ff a, ff b) {
+  ff s = two_sum(a.h, b.h);
+  return {s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l))};
+}
 __device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
 
 __device__ __forceinline__ ff ff_mul(ff a, ff b) {
@@ -140,6 +150,22 @@ template <class S> struct cx_align { static constexpr int value = 2 * sizeof(S);
 template <class S> struct alignas(cx_align<S>::value) cx {
   S r, i;
 };
+
+// butterfly additions: float-float skips the renormalisation (ff_add_nn)
+template <class S> struct bfly {
+  static __device__ __forceinline__ S add(S a, S b) { return sc<S>::add(a, b); }
+  static __device__ __forceinline__ S sub(S a, S b) { return sc<S>::sub(a, b); }
+};
+template <> struct bfly<ff> {
+  static __device__ __forceinline__ ff add(ff a, ff b) { return ff_add_nn(a, b); }
+  static __device__ __forceinline__ ff sub(ff a, ff b) { return ff_add_nn(a, ff_neg(b)); }
+};
+template <class S> __device__ __forceinline__ cx<S> badd(cx<S> a, cx<S> b) {
+  return {bfly<S>::add(a.r, b.r), bfly<S>::add(a.i, b.i)};
+}
+template <class S> __device__ __forceinline__ cx<S> bsub(cx<S> a, cx<S> b) {
+  return {bfly<S>::sub(a.r, b.r), bfly<S>::sub(a.i, b.i)};
+}
 
 template <class S> __device__ __forceinline__ cx<S> cadd(cx<S> a, cx<S> b) {
   return {sc<S>::add(a.r, b.r), sc<S>::add(a.i, b.i)};

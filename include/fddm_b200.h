@@ -101,6 +101,21 @@ int fddm_b200_ddm_diff(const void* d_img_seq, int dtype, uint64_t length, uint64
                        const double* d_window, double* d_out, void* d_workspace, size_t workspace_bytes,
                        int precision, void* stream);
 
+/* Image structure function from frames in HOST memory, with the upload
+   overlapped with the computation (the reference's cores take host arrays:
+   src/cpp/ddm.h:38-61).  The frames are copied chunk by chunk from h_img_seq
+   into the caller's device buffer d_frames (length*height*width elements) on a
+   library copy stream; each chunk's spatial FFTs wait only for that chunk.  With
+   page-locked host memory the copies run concurrently with the kernels.  If
+   h_out is not NULL the result is also copied to it on `stream` at the end.
+   mode is FDDM_MODE_FFT or FDDM_MODE_DIFF (nt ignored for diff); the other
+   arguments as fddm_b200_ddm_fft.  The host buffers must stay valid until the
+   work on `stream` has completed. */
+int fddm_b200_ddm_from_host(int mode, const void* h_img_seq, int dtype, uint64_t length, uint64_t height,
+                            uint64_t width, const uint32_t* lags, uint64_t nlags, uint64_t nx, uint64_t ny,
+                            uint64_t nt, void* d_frames, const double* d_window, double* d_out, double* h_out,
+                            void* d_workspace, size_t workspace_bytes, int precision, void* stream);
+
 /* Weighted azimuthal average of a stack of half-plane maps: the per-(bin, row)
    weighted mean and unbiased weighted standard deviation.  Replaces the two
    per-pixel loops of azimuthal_average_array (src/python/azimuthalaverage.py:435-444

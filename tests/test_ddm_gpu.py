@@ -190,3 +190,19 @@ def test_backend_function_contract(fddm):
     assert out.dtype == np.float64 and out.shape == (4, 12, 9)
     out2 = fddm._backend["b200"]["diff"](imgs, lags, 16, 12, np.array([], dtype=np.float64), gpu_id=0)
     assert oracle.rel_err(out, out2) < 1e-9
+
+
+@pytest.mark.parametrize("mode", ["fft", "diff"])
+def test_input_paths_agree(fddm, mode):
+    """Pageable numpy, page-locked CPU tensor (overlapped upload) and CUDA tensor inputs give identical results."""
+    import torch
+
+    imgs = _poisson_stack((48, 40, 56), "uint16", seed=11)
+    lags = [1, 2, 3, 7, 20, 47]
+    a = fddm.ddm(imgs, lags, mode=mode)._data
+    pinned = torch.from_numpy(imgs.astype(np.int32)).to(torch.int16).pin_memory()
+    b = fddm.ddm(pinned, lags, mode=mode)._data
+    c = fddm.ddm(pinned.cuda(), lags, mode=mode)._data
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a, c)
+    _check(a, imgs, lags, mode, "ff", label="input paths")
