@@ -135,6 +135,29 @@ template <class A> __device__ __forceinline__ A block_exclusive_scan(A v, A* scr
 }
 
 // ---------------------------------------------------------------------------
+// Asynchronous global -> shared copies (cp.async), used to prefetch the next
+// mode's time series while the current one is being transformed.
+// ---------------------------------------------------------------------------
+template <int B> __device__ __forceinline__ void cp_async(void* smem, const void* gmem);
+template <> __device__ __forceinline__ void cp_async<16>(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+template <> __device__ __forceinline__ void cp_async<8>(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Start copying one mode's T values into the (swizzled) transform buffer.
+template <class S>
+__device__ __forceinline__ void prefetch_series(cx<S>* buf, const cx<S>* src, int T, int tid, int nthr) {
+  for (int t = tid; t < T; t += nthr) cp_async<sizeof(cx<S>)>(&buf[swz<S>(t)], src + t);
+  cp_async_commit();
+}
+
+// ---------------------------------------------------------------------------
 // Stage 0: window (FP64) -> S, once per call
 // ---------------------------------------------------------------------------
 template <class S> __global__ void k_window_convert(const double* __restrict__ w, S* __restrict__ out, size_t n) {
@@ -312,11 +335,11 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
     slotA[t] = (short)a.slotA[t];
     slotB[t] = (short)a.slotB[t];
   }
-  __syncthreads();
+  if (blockIdx.x < a.Q) prefetch_series<S>(buf, F + (size_t)blockIdx.x * a.Tpad, T, tid, nthr);
 
   for (size_t q = blockIdx.x; q < a.Q; q += gridDim.x) {
-    const cx<S>* src = F + q * a.Tpad;
-    for (int t = tid; t < N; t += nthr) buf[swz<S>(t)] = t < T ? src[t] : czero<S>();
+    // this mode's series was prefetched into buf[0, T); buf[T, N) is never read
+    cp_async_wait_all();
     __syncthreads();
 
     A v[3] = {sc<A>::zero(), sc<A>::zero(), sc<A>::zero()};
@@ -357,7 +380,7 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
     if (tid == 0 && slotB[0] >= 0) need[nl + slotB[0]] = sc<A>::zero();
     __syncthreads();
 
-    fft_forward<S>(buf, 1, N, a.pt, tw, tid, nthr);
+    fft_forward_padded<S>(buf, a.pt, T, tw, tid, nthr);
     // P(k) = |X(k)|^2 scattered into z as the real sequence z[k/2].{r,i}
     for (int p = tid; p < N; p += nthr) {
       const cx<S> x = buf[swz<S>(p)];
@@ -368,6 +391,8 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
       else e->r = pv;
     }
     __syncthreads();
+    // buf is free until the next iteration: start loading the next mode
+    if (q + gridDim.x < a.Q) prefetch_series<S>(buf, F + (q + gridDim.x) * a.Tpad, T, tid, nthr);
     fft_forward<S>(z, 1, N2, a.pt2, tw2, tid, nthr);
 
     for (int l = tid; l < nl; l += nthr) {

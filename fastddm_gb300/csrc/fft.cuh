@@ -64,10 +64,10 @@ template <class S, bool INV> __device__ __forceinline__ void dft4(cx<S>* v) {
   dft4_vals<S, INV>(v[0], v[1], v[2], v[3]);
 }
 
-template <class S, bool INV> __device__ __forceinline__ void dft8(cx<S>* v) {
+template <class S, bool INV>
+__device__ __forceinline__ void dft8_tail(cx<S>* v, cx<S> a0, cx<S> a1, cx<S> a2, cx<S> a3, cx<S> b0, cx<S> b1,
+                                          cx<S> b2, cx<S> b3) {
   const S h = sc<S>::cst(kSqrtHalfH, kSqrtHalfL, kSqrtHalfD);
-  cx<S> a0 = badd(v[0], v[4]), a1 = badd(v[1], v[5]), a2 = badd(v[2], v[6]), a3 = badd(v[3], v[7]);
-  cx<S> b0 = bsub(v[0], v[4]), b1 = bsub(v[1], v[5]), b2 = bsub(v[2], v[6]), b3 = bsub(v[3], v[7]);
   // b_r *= w8^r  (forward w8 = (1 - i)/sqrt2, inverse its conjugate)
   if (!INV) {
     b1 = cscale<S>({bfly<S>::add(b1.r, b1.i), bfly<S>::sub(b1.i, b1.r)}, h);
@@ -81,6 +81,16 @@ template <class S, bool INV> __device__ __forceinline__ void dft8(cx<S>* v) {
   dft4_vals<S, INV>(b0, b1, b2, b3);
   v[0] = a0; v[2] = a1; v[4] = a2; v[6] = a3;
   v[1] = b0; v[3] = b1; v[5] = b2; v[7] = b3;
+}
+
+template <class S, bool INV> __device__ __forceinline__ void dft8(cx<S>* v) {
+  dft8_tail<S, INV>(v, badd(v[0], v[4]), badd(v[1], v[5]), badd(v[2], v[6]), badd(v[3], v[7]), bsub(v[0], v[4]),
+                    bsub(v[1], v[5]), bsub(v[2], v[6]), bsub(v[3], v[7]));
+}
+
+// radix 8 with v[4..7] == 0 (the upper half of a zero-padded input)
+template <class S, bool INV> __device__ __forceinline__ void dft8_halfzero(cx<S>* v) {
+  dft8_tail<S, INV>(v, v[0], v[1], v[2], v[3], v[0], v[1], v[2], v[3]);
 }
 
 // Odd radix via conjugate-pair symmetry: R^2/4 complex-by-real products.
@@ -211,6 +221,52 @@ __device__ __forceinline__ void fft_pass_dispatch(cx<S>* buf, int nfft, int ld, 
     case 11: fft_pass<S, 11, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
     case 13: fft_pass<S, 13, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
     default: break;
+  }
+}
+
+// First forward pass of a single transform whose input is zero at indices >=
+// `limit` (limit <= n/2): those slots are neither loaded nor need to be
+// written beforehand.  With radix 8 the upper half of every butterfly is zero,
+// so its first add/sub stage is skipped.
+template <class S, int R>
+__device__ __forceinline__ void fft_first_pass_padded(cx<S>* __restrict__ buf, const FftPlan& p, int limit,
+                                                      const cx<S>* __restrict__ tw, int tid, int nthr) {
+  const int n = p.n, stride = n / R;
+  for (int j = tid; j < stride; j += nthr) {
+    cx<S> v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int idx = j + r * stride;
+      v[r] = (r < R / 2 || R % 2) && idx < limit ? buf[swz<S>(idx)] : czero<S>();
+    }
+    if constexpr (R == 8) dft8_halfzero<S, false>(v);
+    else dft<S, R, false>(v);
+    if (j != 0) {
+#pragma unroll
+      for (int m = 1; m < R; ++m) v[m] = cmul(v[m], tw[j * m]);
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) buf[swz<S>(j + r * stride)] = v[r];
+  }
+}
+
+// Forward transform of a zero-padded input (zeros at indices >= limit, limit <= n/2).
+template <class S>
+__device__ void fft_forward_padded(cx<S>* buf, const FftPlan& p, int limit, const cx<S>* tw, int tid, int nthr) {
+  switch (p.radix[0]) {
+    case 2: fft_first_pass_padded<S, 2>(buf, p, limit, tw, tid, nthr); break;
+    case 3: fft_first_pass_padded<S, 3>(buf, p, limit, tw, tid, nthr); break;
+    case 4: fft_first_pass_padded<S, 4>(buf, p, limit, tw, tid, nthr); break;
+    case 5: fft_first_pass_padded<S, 5>(buf, p, limit, tw, tid, nthr); break;
+    case 7: fft_first_pass_padded<S, 7>(buf, p, limit, tw, tid, nthr); break;
+    case 8: fft_first_pass_padded<S, 8>(buf, p, limit, tw, tid, nthr); break;
+    case 11: fft_first_pass_padded<S, 11>(buf, p, limit, tw, tid, nthr); break;
+    default: fft_first_pass_padded<S, 13>(buf, p, limit, tw, tid, nthr); break;
+  }
+  __syncthreads();
+  for (int s = 1; s < p.npass; ++s) {
+    fft_pass_dispatch<S, false>(buf, 1, p.n, p, s, tw, tid, nthr);
+    __syncthreads();
   }
 }
 
