@@ -166,106 +166,165 @@ template <class S> __global__ void k_window_convert(const double* __restrict__ w
 }
 
 // ---------------------------------------------------------------------------
-// Stage 1: row pass
-// grid (ceil(npairs / pairs_per_block), frames in chunk); dynamic smem pairs*nx*cx<S>
+// Stage 1: row pass.  Persistent CTAs walk the items (group of row pairs,
+// frame) of one frame chunk.  When rows are 16-byte aligned the raw pixels of
+// the next item are copied with cp.async into a double-buffered staging area
+// while the current item is transformed.
+// dynamic smem: swz_round(pairs * nx) * cx<S> [+ 2 * raw_stage_bytes]
 // ---------------------------------------------------------------------------
+template <class S, class IN>
+__device__ __forceinline__ void rows_issue_raw(const SpatialArgs& a, int item, unsigned char* raw, int ngroups,
+                                               int tid, int nthr) {
+  const int g = item % ngroups, tl = item / ngroups;
+  const int pair0 = g * a.pairs_per_block;
+  const int npairs = (a.H + 1) >> 1;
+  const int np = min(a.pairs_per_block, npairs - pair0);
+  const int y0 = 2 * pair0;
+  const int rows = min(2 * np, a.H - y0);
+  const int cpr = a.W * (int)sizeof(IN) / 16;  // 16-byte chunks per row
+  const unsigned char* src = reinterpret_cast<const unsigned char*>(a.img) +
+                             ((size_t)(a.t0 + tl) * a.H + y0) * (size_t)a.W * sizeof(IN);
+  for (int c = tid; c < rows * cpr; c += nthr) cp_async<16>(raw + (size_t)c * 16, src + (size_t)c * 16);
+  cp_async_commit();
+}
+
 template <class S, class IN>
 __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
   const int nx = a.nx, W = a.W, H = a.H;
   const int npairs = (H + 1) >> 1;
-  const int pair0 = blockIdx.x * a.pairs_per_block;
-  const int np = min(a.pairs_per_block, npairs - pair0);
-  const int tl = blockIdx.y;
-  const size_t t = (size_t)a.t0 + tl;
-  const IN* img = reinterpret_cast<const IN*>(a.img) + t * (size_t)H * W;
+  const int ngroups = (npairs + a.pairs_per_block - 1) / a.pairs_per_block;
+  const int nitems = ngroups * a.tc;
   const S* win = reinterpret_cast<const S*>(a.window_s);
   const int tid = threadIdx.x, nthr = blockDim.x;
-
-  for (int e = tid; e < np * nx; e += nthr) {
-    const int p = e / nx;
-    const int x = e - p * nx;
-    const int y0 = 2 * (pair0 + p);
-    S va = sc<S>::zero(), vb = sc<S>::zero();
-    if (x < W) {
-      va = pix<S, IN>::get(img, (size_t)y0 * W + x);
-      if (win) va = sc<S>::mul(va, win[(size_t)y0 * W + x]);
-      if (y0 + 1 < H) {
-        vb = pix<S, IN>::get(img, (size_t)(y0 + 1) * W + x);
-        if (win) vb = sc<S>::mul(vb, win[(size_t)(y0 + 1) * W + x]);
-      }
-    }
-    buf[swz<S>(p * nx + x)] = {va, vb};
-  }
-  __syncthreads();
-  fft_forward<S>(buf, np, nx, a.px, reinterpret_cast<const cx<S>*>(a.twx), tid, nthr);
-
-  // unpack Z = A + iB into the spectra of the two real rows; write R[tl][k][y]
   const int nkx = a.nkx;
-  const int ny2 = 2 * np;
-  cx<S>* R = reinterpret_cast<cx<S>*>(a.rbuf) + (size_t)tl * nkx * a.Hpad;
-  for (int e = tid; e < ny2 * nkx; e += nthr) {
-    const int k = e / ny2;
-    const int yl = e - k * ny2;
-    const int p = yl >> 1;
-    const cx<S> zk = buf[swz<S>(p * nx + a.permx[k])];
-    const cx<S> zn = buf[swz<S>(p * nx + a.permx[k == 0 ? 0 : nx - k])];
-    cx<S> v;
-    if ((yl & 1) == 0) {
-      v = {sc<S>::half(sc<S>::add(zk.r, zn.r)), sc<S>::half(sc<S>::sub(zk.i, zn.i))};
+  const bool async_raw = a.raw_stage_bytes > 0;
+  unsigned char* raw[2] = {smem_raw + (size_t)swz_round<S>(a.pairs_per_block * nx) * sizeof(cx<S>), nullptr};
+  raw[1] = raw[0] + a.raw_stage_bytes;
+  int b = 0;
+  if (async_raw && (int)blockIdx.x < nitems) rows_issue_raw<S, IN>(a, blockIdx.x, raw[0], ngroups, tid, nthr);
+
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const int g = item % ngroups, tl = item / ngroups;
+    const int pair0 = g * a.pairs_per_block;
+    const int np = min(a.pairs_per_block, npairs - pair0);
+    const size_t t = (size_t)a.t0 + tl;
+    if (async_raw) {
+      cp_async_wait_all();
+      __syncthreads();
+      const int next = item + gridDim.x;
+      if (next < nitems) rows_issue_raw<S, IN>(a, next, raw[b ^ 1], ngroups, tid, nthr);
     } else {
-      v = {sc<S>::half(sc<S>::add(zk.i, zn.i)), sc<S>::half(sc<S>::sub(zn.r, zk.r))};
+      __syncthreads();
     }
-    R[(size_t)k * a.Hpad + 2 * pair0 + yl] = v;
+    const IN* img = reinterpret_cast<const IN*>(a.img) + t * (size_t)H * W;
+    const IN* rimg = reinterpret_cast<const IN*>(raw[b]);
+    for (int e = tid; e < np * nx; e += nthr) {
+      const int p = e / nx;
+      const int x = e - p * nx;
+      const int y0 = 2 * (pair0 + p);
+      S va = sc<S>::zero(), vb = sc<S>::zero();
+      if (x < W) {
+        // staged rows are relative to the group's first row
+        va = async_raw ? pix<S, IN>::get(rimg, (size_t)(2 * p) * W + x) : pix<S, IN>::get(img, (size_t)y0 * W + x);
+        if (win) va = sc<S>::mul(va, win[(size_t)y0 * W + x]);
+        if (y0 + 1 < H) {
+          vb = async_raw ? pix<S, IN>::get(rimg, (size_t)(2 * p + 1) * W + x)
+                         : pix<S, IN>::get(img, (size_t)(y0 + 1) * W + x);
+          if (win) vb = sc<S>::mul(vb, win[(size_t)(y0 + 1) * W + x]);
+        }
+      }
+      buf[swz<S>(p * nx + x)] = {va, vb};
+    }
+    __syncthreads();
+    fft_forward<S>(buf, np, nx, a.px, reinterpret_cast<const cx<S>*>(a.twx), tid, nthr);
+
+    // unpack Z = A + iB into the spectra of the two real rows; write R[tl][k][y]
+    const int ny2 = 2 * np;
+    cx<S>* R = reinterpret_cast<cx<S>*>(a.rbuf) + (size_t)tl * nkx * a.Hpad;
+    for (int e = tid; e < ny2 * nkx; e += nthr) {
+      const int k = e / ny2;
+      const int yl = e - k * ny2;
+      const int p = yl >> 1;
+      const cx<S> zk = buf[swz<S>(p * nx + a.permx[k])];
+      const cx<S> zn = buf[swz<S>(p * nx + a.permx[k == 0 ? 0 : nx - k])];
+      cx<S> v;
+      if ((yl & 1) == 0) {
+        v = {sc<S>::half(sc<S>::add(zk.r, zn.r)), sc<S>::half(sc<S>::sub(zk.i, zn.i))};
+      } else {
+        v = {sc<S>::half(sc<S>::add(zk.i, zn.i)), sc<S>::half(sc<S>::sub(zn.r, zk.r))};
+      }
+      R[(size_t)k * a.Hpad + 2 * pair0 + yl] = v;
+    }
+    b ^= 1;
   }
 }
 
 // ---------------------------------------------------------------------------
-// Stage 2: column pass
-// grid (ceil(nkx / cols_per_block), ceil(frames / frames_per_block))
+// Stage 2: column pass.  Persistent CTAs walk the items (group of columns,
+// group of frames) of one frame chunk; the next item's columns are copied with
+// cp.async into the second of two transform buffers while the current item
+// is transformed.
+// dynamic smem: 2 * swz_round(cols * frames * ny) * cx<S>
 // ---------------------------------------------------------------------------
 template <class S>
-__global__ void __launch_bounds__(256) k_cols(SpatialArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
+__device__ __forceinline__ void cols_issue(const SpatialArgs& a, int item, cx<S>* buf, int ncg, int tid, int nthr) {
   const int ny = a.ny, H = a.H, nkx = a.nkx;
-  const int CK = a.cols_per_block, TG = a.frames_per_block;
-  const int kc0 = blockIdx.x * CK;
-  const int tl0 = blockIdx.y * TG;
-  const int nk = min(CK, nkx - kc0);
-  const int ntg = min(TG, a.tc - tl0);
-  const int NB = CK * TG;
-  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int CK = a.cols_per_block, TG = a.frames_per_block, NB = CK * TG;
+  const int kc0 = (item % ncg) * CK, tl0 = (item / ncg) * TG;
+  const int nk = min(CK, nkx - kc0), ntg = min(TG, a.tc - tl0);
   const cx<S>* R = reinterpret_cast<const cx<S>*>(a.rbuf);
-
   for (int e = tid; e < NB * ny; e += nthr) {
     const int c = e / ny;
     const int y = e - c * ny;
     const int tl = c / CK;
     const int kc = c - tl * CK;
-    cx<S> v = czero<S>();
-    if (kc < nk && tl < ntg && y < H) v = R[((size_t)(tl0 + tl) * nkx + kc0 + kc) * a.Hpad + y];
-    buf[swz<S>(c * ny + y)] = v;
+    cx<S>* dst = &buf[swz<S>(c * ny + y)];
+    if (kc < nk && tl < ntg && y < H) cp_async<sizeof(cx<S>)>(dst, &R[((size_t)(tl0 + tl) * nkx + kc0 + kc) * a.Hpad + y]);
+    else *dst = czero<S>();
   }
-  __syncthreads();
-  fft_forward<S>(buf, NB, ny, a.py, reinterpret_cast<const cx<S>*>(a.twy), tid, nthr);
+  cp_async_commit();
+}
 
+template <class S>
+__global__ void __launch_bounds__(512) k_cols(SpatialArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ny = a.ny, nkx = a.nkx;
+  const int CK = a.cols_per_block, TG = a.frames_per_block, NB = CK * TG;
+  const int ncg = (nkx + CK - 1) / CK;
+  const int nitems = ncg * ((a.tc + TG - 1) / TG);
+  cx<S>* bufs[2] = {reinterpret_cast<cx<S>*>(smem_raw), reinterpret_cast<cx<S>*>(smem_raw) + swz_round<S>(NB * ny)};
+  const int tid = threadIdx.x, nthr = blockDim.x;
   const S norm = sc<S>::cst(a.norm_h, a.norm_l, a.norm_d);
   cx<S>* F = reinterpret_cast<cx<S>*>(a.spec);
   const int half = ny >> 1;
-  for (int e = tid; e < NB * ny; e += nthr) {
-    const int tl = e % TG;
-    const int rest = e / TG;
-    const int kc = rest % CK;
-    const int ky = rest / CK;
-    if (tl < ntg && kc < nk) {
-      const cx<S> v = cscale(buf[swz<S>((tl * CK + kc) * ny + a.permy[ky])], norm);
-      int ys = ky + half;
-      if (ys >= ny) ys -= ny;
-      const size_t q = (size_t)ys * nkx + kc0 + kc;
-      F[q * a.Tpad + a.t0 + tl0 + tl] = v;
+  int b = 0;
+  if ((int)blockIdx.x < nitems) cols_issue<S>(a, blockIdx.x, bufs[0], ncg, tid, nthr);
+
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    cp_async_wait_all();
+    __syncthreads();
+    const int next = item + gridDim.x;
+    if (next < nitems) cols_issue<S>(a, next, bufs[b ^ 1], ncg, tid, nthr);
+    cx<S>* buf = bufs[b];
+    const int kc0 = (item % ncg) * CK, tl0 = (item / ncg) * TG;
+    const int nk = min(CK, nkx - kc0), ntg = min(TG, a.tc - tl0);
+    fft_forward<S>(buf, NB, ny, a.py, reinterpret_cast<const cx<S>*>(a.twy), tid, nthr);
+    for (int e = tid; e < NB * ny; e += nthr) {
+      const int tl = e % TG;
+      const int rest = e / TG;
+      const int kc = rest % CK;
+      const int ky = rest / CK;
+      if (tl < ntg && kc < nk) {
+        const cx<S> v = cscale(buf[swz<S>((tl * CK + kc) * ny + a.permy[ky])], norm);
+        int ys = ky + half;
+        if (ys >= ny) ys -= ny;
+        const size_t q = (size_t)ys * nkx + kc0 + kc;
+        F[q * a.Tpad + a.t0 + tl0 + tl] = v;
+      }
     }
+    b ^= 1;
   }
 }
 

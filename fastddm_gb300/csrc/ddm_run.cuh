@@ -32,24 +32,33 @@ inline int temporal_threads(int n) {
   return t;
 }
 
+// Persistent grid: as many CTAs as fit on the device, at most one per item.
+template <class K> inline unsigned persistent_grid(K kernel, int threads, size_t smem, int items) {
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem);
+  return (unsigned)std::max(1, std::min(items, std::max(occ, 1) * nsm));
+}
+
 template <class S, class IN>
-cudaError_t launch_rows(const SpatialArgs& a, dim3 grid, size_t smem, cudaStream_t st) {
+cudaError_t launch_rows(const SpatialArgs& a, int items, size_t smem, cudaStream_t st) {
   cudaError_t e = allow_smem(k_rows<S, IN>, smem);
   if (e != cudaSuccess) return e;
-  k_rows<S, IN><<<grid, 256, smem, st>>>(a);
+  k_rows<S, IN><<<persistent_grid(k_rows<S, IN>, 256, smem, items), 256, smem, st>>>(a);
   return cudaGetLastError();
 }
 
 template <class S>
-cudaError_t dispatch_rows(int dtype, const SpatialArgs& a, dim3 grid, size_t smem, cudaStream_t st) {
+cudaError_t dispatch_rows(int dtype, const SpatialArgs& a, int items, size_t smem, cudaStream_t st) {
   switch (dtype) {
-    case DT_U8: return launch_rows<S, uint8_t>(a, grid, smem, st);
-    case DT_I16: return launch_rows<S, int16_t>(a, grid, smem, st);
-    case DT_U16: return launch_rows<S, uint16_t>(a, grid, smem, st);
-    case DT_I32: return launch_rows<S, int32_t>(a, grid, smem, st);
-    case DT_U32: return launch_rows<S, uint32_t>(a, grid, smem, st);
-    case DT_F32: return launch_rows<S, float>(a, grid, smem, st);
-    case DT_F64: return launch_rows<S, double>(a, grid, smem, st);
+    case DT_U8: return launch_rows<S, uint8_t>(a, items, smem, st);
+    case DT_I16: return launch_rows<S, int16_t>(a, items, smem, st);
+    case DT_U16: return launch_rows<S, uint16_t>(a, items, smem, st);
+    case DT_I32: return launch_rows<S, int32_t>(a, items, smem, st);
+    case DT_U32: return launch_rows<S, uint32_t>(a, items, smem, st);
+    case DT_F32: return launch_rows<S, float>(a, items, smem, st);
+    case DT_F64: return launch_rows<S, double>(a, items, smem, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -159,8 +168,14 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   split_ff(norm, sa.norm_h, sa.norm_l);
   sa.norm_d = norm;
   const int npairs = (H + 1) / 2;
-  const size_t smem_rows = (size_t)swz_round<S>(L.pairs_per_block * nx) * sizeof(cx<S>);
-  const size_t smem_cols = (size_t)swz_round<S>(L.cols_per_block * L.frames_per_block * ny) * sizeof(cx<S>);
+  // raw rows staged asynchronously when every row starts on a 16-byte boundary
+  const size_t row_bytes = (size_t)W * dtype_bytes(r.dtype);
+  const size_t stage = (size_t)2 * L.pairs_per_block * row_bytes;
+  sa.raw_stage_bytes = (row_bytes % 16 == 0 && (reinterpret_cast<uintptr_t>(r.img) % 16) == 0 && 2 * stage <= 64 * 1024)
+                           ? (int)stage : 0;
+  const size_t smem_rows = (size_t)swz_round<S>(L.pairs_per_block * nx) * sizeof(cx<S>) + 2 * (size_t)sa.raw_stage_bytes;
+  const size_t smem_cols = 2 * (size_t)swz_round<S>(L.cols_per_block * L.frames_per_block * ny) * sizeof(cx<S>);
+  const int ngroups = (npairs + L.pairs_per_block - 1) / L.pairs_per_block;
   if ((ce = allow_smem(k_cols<S>, smem_cols)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
   CopyCtx* cp = nullptr;
   const size_t frame_bytes = (size_t)H * W * dtype_bytes(r.dtype);
@@ -186,10 +201,13 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
         return 3;
       }
     }
-    dim3 gr((npairs + L.pairs_per_block - 1) / L.pairs_per_block, sa.tc);
-    if ((ce = dispatch_rows<S>(r.dtype, sa, gr, smem_rows, st)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
-    dim3 gc((nkx + L.cols_per_block - 1) / L.cols_per_block, (sa.tc + L.frames_per_block - 1) / L.frames_per_block);
-    k_cols<S><<<gc, 256, smem_cols, st>>>(sa);
+    if ((ce = dispatch_rows<S>(r.dtype, sa, ngroups * sa.tc, smem_rows, st)) != cudaSuccess) {
+      err = cudaGetErrorString(ce);
+      return 3;
+    }
+    const int col_items = ((nkx + L.cols_per_block - 1) / L.cols_per_block) *
+                          ((sa.tc + L.frames_per_block - 1) / L.frames_per_block);
+    k_cols<S><<<persistent_grid(k_cols<S>, 512, smem_cols, col_items), 512, smem_cols, st>>>(sa);
     if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
     launches += 2;
   }

@@ -27,6 +27,7 @@ struct SpatialArgs {
   int t0, tc;            // first frame and number of frames of this chunk
   int Tpad;              // spectrum row stride (elements)
   int pairs_per_block, cols_per_block, frames_per_block;
+  int raw_stage_bytes;   // >0: rows are staged with cp.async (16-byte aligned rows)
   FftPlan px, py;
   const void* twx;
   const void* twy;

@@ -234,7 +234,8 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
   const int nb = (int)std::max<size_t>(1, target / ((size_t)r.ny * es));
   L.frames_per_block = std::min(nb, 8);
   L.cols_per_block = std::max(1, nb / L.frames_per_block);
-  if ((size_t)(L.pairs_per_block * r.nx + 16) * es > kSmemLimit || (size_t)(nb * r.ny + 16) * es > kSmemLimit) {
+  // row pass: one transform buffer (+ at most 64 KB of raw staging); column pass: two buffers
+  if ((size_t)(L.pairs_per_block * r.nx + 16) * es + 65536 > kSmemLimit || (size_t)(2 * nb * r.ny + 32) * es > kSmemLimit) {
     err = "image dimensions too large for the shared-memory FFT";
     return false;
   }
