@@ -200,7 +200,11 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nkx = a.nkx;
   const bool async_raw = a.raw_stage_bytes > 0;
-  unsigned char* raw[2] = {smem_raw + (size_t)swz_round<S>(a.pairs_per_block * nx) * sizeof(cx<S>), nullptr};
+  // transforms are laid out with a stride of nx plus one swizzle group, so the
+  // unpack phase (several transforms read at the same permuted slot) hits
+  // different banks
+  const int ld = nx + swz_group<S>::G;
+  unsigned char* raw[2] = {smem_raw + (size_t)swz_round<S>(a.pairs_per_block * ld) * sizeof(cx<S>), nullptr};
   raw[1] = raw[0] + a.raw_stage_bytes;
   int b = 0;
   if (async_raw && (int)blockIdx.x < nitems) rows_issue_raw<S, IN>(a, blockIdx.x, raw[0], ngroups, tid, nthr);
@@ -235,20 +239,21 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
           if (win) vb = sc<S>::mul(vb, win[(size_t)(y0 + 1) * W + x]);
         }
       }
-      buf[swz<S>(p * nx + x)] = {va, vb};
+      buf[swz<S>(p * ld + x)] = {va, vb};
     }
     __syncthreads();
-    fft_forward<S>(buf, np, nx, a.px, reinterpret_cast<const cx<S>*>(a.twx), tid, nthr);
+    fft_forward<S>(buf, np, ld, a.px, reinterpret_cast<const cx<S>*>(a.twx), tid, nthr);
 
     // unpack Z = A + iB into the spectra of the two real rows; write R[tl][k][y]
     const int ny2 = 2 * np;
+    const int lg2 = (ny2 & (ny2 - 1)) == 0 ? __ffs(ny2) - 1 : -1;
     cx<S>* R = reinterpret_cast<cx<S>*>(a.rbuf) + (size_t)tl * nkx * a.Hpad;
     for (int e = tid; e < ny2 * nkx; e += nthr) {
-      const int k = e / ny2;
+      const int k = lg2 >= 0 ? e >> lg2 : e / ny2;
       const int yl = e - k * ny2;
       const int p = yl >> 1;
-      const cx<S> zk = buf[swz<S>(p * nx + a.permx[k])];
-      const cx<S> zn = buf[swz<S>(p * nx + a.permx[k == 0 ? 0 : nx - k])];
+      const cx<S> zk = buf[swz<S>(p * ld + a.permx[k])];
+      const cx<S> zn = buf[swz<S>(p * ld + a.permx[k == 0 ? 0 : nx - k])];
       cx<S> v;
       if ((yl & 1) == 0) {
         v = {sc<S>::half(sc<S>::add(zk.r, zn.r)), sc<S>::half(sc<S>::sub(zk.i, zn.i))};
@@ -269,7 +274,8 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
 // dynamic smem: 2 * swz_round(cols * frames * ny) * cx<S>
 // ---------------------------------------------------------------------------
 template <class S>
-__device__ __forceinline__ void cols_issue(const SpatialArgs& a, int item, cx<S>* buf, int ncg, int tid, int nthr) {
+__device__ __forceinline__ void cols_issue(const SpatialArgs& a, int item, cx<S>* buf, int ncg, int ld, int tid,
+                                           int nthr) {
   const int ny = a.ny, H = a.H, nkx = a.nkx;
   const int CK = a.cols_per_block, TG = a.frames_per_block, NB = CK * TG;
   const int kc0 = (item % ncg) * CK, tl0 = (item / ncg) * TG;
@@ -280,7 +286,7 @@ __device__ __forceinline__ void cols_issue(const SpatialArgs& a, int item, cx<S>
     const int y = e - c * ny;
     const int tl = c / CK;
     const int kc = c - tl * CK;
-    cx<S>* dst = &buf[swz<S>(c * ny + y)];
+    cx<S>* dst = &buf[swz<S>(c * ld + y)];
     if (kc < nk && tl < ntg && y < H) cp_async<sizeof(cx<S>)>(dst, &R[((size_t)(tl0 + tl) * nkx + kc0 + kc) * a.Hpad + y]);
     else *dst = czero<S>();
   }
@@ -294,30 +300,32 @@ __global__ void __launch_bounds__(512) k_cols(SpatialArgs a) {
   const int CK = a.cols_per_block, TG = a.frames_per_block, NB = CK * TG;
   const int ncg = (nkx + CK - 1) / CK;
   const int nitems = ncg * ((a.tc + TG - 1) / TG);
-  cx<S>* bufs[2] = {reinterpret_cast<cx<S>*>(smem_raw), reinterpret_cast<cx<S>*>(smem_raw) + swz_round<S>(NB * ny)};
+  const int ld = ny + swz_group<S>::G;  // padded stride: the store phase reads NB transforms at one slot
+  cx<S>* bufs[2] = {reinterpret_cast<cx<S>*>(smem_raw), reinterpret_cast<cx<S>*>(smem_raw) + swz_round<S>(NB * ld)};
+  const int lgTG = (TG & (TG - 1)) == 0 ? __ffs(TG) - 1 : -1;
+  const int lgCK = (CK & (CK - 1)) == 0 ? __ffs(CK) - 1 : -1;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const S norm = sc<S>::cst(a.norm_h, a.norm_l, a.norm_d);
   cx<S>* F = reinterpret_cast<cx<S>*>(a.spec);
   const int half = ny >> 1;
   int b = 0;
-  if ((int)blockIdx.x < nitems) cols_issue<S>(a, blockIdx.x, bufs[0], ncg, tid, nthr);
+  if ((int)blockIdx.x < nitems) cols_issue<S>(a, blockIdx.x, bufs[0], ncg, ld, tid, nthr);
 
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     cp_async_wait_all();
     __syncthreads();
     const int next = item + gridDim.x;
-    if (next < nitems) cols_issue<S>(a, next, bufs[b ^ 1], ncg, tid, nthr);
+    if (next < nitems) cols_issue<S>(a, next, bufs[b ^ 1], ncg, ld, tid, nthr);
     cx<S>* buf = bufs[b];
     const int kc0 = (item % ncg) * CK, tl0 = (item / ncg) * TG;
     const int nk = min(CK, nkx - kc0), ntg = min(TG, a.tc - tl0);
-    fft_forward<S>(buf, NB, ny, a.py, reinterpret_cast<const cx<S>*>(a.twy), tid, nthr);
+    fft_forward<S>(buf, NB, ld, a.py, reinterpret_cast<const cx<S>*>(a.twy), tid, nthr);
     for (int e = tid; e < NB * ny; e += nthr) {
-      const int tl = e % TG;
-      const int rest = e / TG;
-      const int kc = rest % CK;
-      const int ky = rest / CK;
+      int tl, rest, kc, ky;
+      if (lgTG >= 0) { tl = e & (TG - 1); rest = e >> lgTG; } else { tl = e % TG; rest = e / TG; }
+      if (lgCK >= 0) { kc = rest & (CK - 1); ky = rest >> lgCK; } else { kc = rest % CK; ky = rest / CK; }
       if (tl < ntg && kc < nk) {
-        const cx<S> v = cscale(buf[swz<S>((tl * CK + kc) * ny + a.permy[ky])], norm);
+        const cx<S> v = cscale(buf[swz<S>((tl * CK + kc) * ld + a.permy[ky])], norm);
         int ys = ky + half;
         if (ys >= ny) ys -= ny;
         const size_t q = (size_t)ys * nkx + kc0 + kc;

@@ -173,8 +173,9 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   const size_t stage = (size_t)2 * L.pairs_per_block * row_bytes;
   sa.raw_stage_bytes = (row_bytes % 16 == 0 && (reinterpret_cast<uintptr_t>(r.img) % 16) == 0 && 2 * stage <= 64 * 1024)
                            ? (int)stage : 0;
-  const size_t smem_rows = (size_t)swz_round<S>(L.pairs_per_block * nx) * sizeof(cx<S>) + 2 * (size_t)sa.raw_stage_bytes;
-  const size_t smem_cols = 2 * (size_t)swz_round<S>(L.cols_per_block * L.frames_per_block * ny) * sizeof(cx<S>);
+  const int G = swz_group<S>::G;
+  const size_t smem_rows = (size_t)swz_round<S>(L.pairs_per_block * (nx + G)) * sizeof(cx<S>) + 2 * (size_t)sa.raw_stage_bytes;
+  const size_t smem_cols = 2 * (size_t)swz_round<S>(L.cols_per_block * L.frames_per_block * (ny + G)) * sizeof(cx<S>);
   const int ngroups = (npairs + L.pairs_per_block - 1) / L.pairs_per_block;
   if ((ce = allow_smem(k_cols<S>, smem_cols)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
   CopyCtx* cp = nullptr;

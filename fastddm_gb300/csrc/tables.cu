@@ -228,14 +228,22 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
   const size_t Q = (size_t)r.ny * nkx;
   L.Tpad = (int)align_up((size_t)r.T, 64 / es);
   L.Hpad = (int)(2 * ((r.H + 1) / 2));
-  // stage 1-2 blocking: ~64 KB of shared memory per CTA
+  // stage 1-2 blocking: ~64 KB of shared memory per transform buffer; every
+  // transform is padded by one swizzle group (128 bytes)
   const size_t target = 64 * 1024;
+  const size_t g = 128 / es;
   L.pairs_per_block = (int)std::max<size_t>(1, std::min<size_t>(target / ((size_t)r.nx * es), (size_t)((r.H + 1) / 2)));
   const int nb = (int)std::max<size_t>(1, target / ((size_t)r.ny * es));
   L.frames_per_block = std::min(nb, 8);
   L.cols_per_block = std::max(1, nb / L.frames_per_block);
-  // row pass: one transform buffer (+ at most 64 KB of raw staging); column pass: two buffers
-  if ((size_t)(L.pairs_per_block * r.nx + 16) * es + 65536 > kSmemLimit || (size_t)(2 * nb * r.ny + 32) * es > kSmemLimit) {
+  auto cols_bytes = [&] {
+    return (size_t)(2 * (L.frames_per_block * L.cols_per_block * (r.ny + g) + g)) * es;
+  };
+  while (cols_bytes() > kSmemLimit && L.cols_per_block > 1) L.cols_per_block /= 2;
+  while (cols_bytes() > kSmemLimit && L.frames_per_block > 1) L.frames_per_block /= 2;
+  // row pass: one transform buffer + at most 64 KB of raw staging; column pass: two buffers
+  if ((size_t)(L.pairs_per_block * (r.nx + g) + g) * es + 65536 > kSmemLimit ||
+      (size_t)(2 * (L.frames_per_block * L.cols_per_block * (r.ny + g) + g)) * es > kSmemLimit) {
     err = "image dimensions too large for the shared-memory FFT";
     return false;
   }
