@@ -36,6 +36,8 @@ CONFIGS = {
     "small": "CONFIG1",        # 64 x 128^2 uint16, all lags
     "large_tall": "CONFIG3_TALL",  # profiling: the large workload's temporal kernel on 64^2 frames
     "large_wide": "CONFIG3_WIDE",  # profiling: the large workload's spatial kernels on 64 frames
+    "batch": None,             # 96 uneven stacks in one batch call (run_batch)
+    "serve": None,             # Poisson request stream through the serving loop (run_serve)
 }
 
 
@@ -452,6 +454,143 @@ def run_validate(args):
                       "lags": int(len(lags)), "errors": results}))
 
 
+def _clock_block(clk):
+    return clk.summary() if clk is not None else None
+
+
+def run_batch(args):
+    """96 uneven stacks (sides 64..512, 100..2000 frames, uint16, all lags) in one batch call."""
+    import torch
+
+    from fastddm_gb300 import _build, _lib, synthetic, batch as fb
+    from fastddm_gb300._ddm_b200 import DdmPlan
+
+    _build.build()
+    lib = _lib.load()
+    device = torch.device("cuda", 0)
+    scenes = synthetic.config4_scenes(96, seed=0)
+    jobs = []
+    for sc in scenes:
+        frames = synthetic.make_stack_torch(sc, device=device)
+        jobs.append(fb.make_job(frames, np.arange(1, sc.length), mode=args.mode, device=device))
+    total_frames = sum(sc.length for sc in scenes)
+    plan = fb.BatchPlan(jobs, args.precision, device)
+    stream = torch.cuda.current_stream(device)
+    for _ in range(args.warmup):
+        plan.run(stream)
+    torch.cuda.synchronize(device)
+    l0 = lib.fddm_b200_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            plan.run(stream)
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = int(lib.fddm_b200_launch_count() - l0)
+    value = total_frames / (ms / 1000.0)
+    # the same jobs one at a time on one stream
+    del plan
+    torch.cuda.empty_cache()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for j in jobs:
+        p = DdmPlan(j.mode, *j.shape, j.dtype_code, j.lags, j.nx, j.ny, j.nt, False, args.precision, device)
+        p.run(j.frames, None, j.out, stream)
+        stream.synchronize()
+        del p
+    t1.record(stream)
+    torch.cuda.synchronize(device)
+    seq_ms = t0.elapsed_time(t1)
+    line = {
+        "metric": "DDM frames/s (batched uneven stacks)", "value": value, "unit": "frames/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.precision, "data": "synthetic",
+        "config": {"workload": f"batch_{len(scenes)}_stacks_{total_frames}_frames_all_lags", "stacks": len(scenes),
+                   "frames": total_frames, "mode": args.mode, "precision": args.precision,
+                   "sides": sorted({sc.height for sc in scenes}), "frames_range": [min(s.length for s in scenes),
+                                                                                   max(s.length for s in scenes)]},
+        "one_at_a_time": {"value": total_frames / (seq_ms / 1000.0), "ms": seq_ms},
+        "clocks": _clock_block(clk), "gpu_launches": launches,
+    }
+    print(json.dumps(line))
+
+
+def run_serve(args):
+    """Poisson arrivals (50 req/s) of config-4-sized jobs plus 5 % 1024^2 x 2000 jobs."""
+    import torch
+
+    from fastddm_gb300 import _build, synthetic
+    from fastddm_gb300._ddm_b200 import DdmPlan
+    from fastddm_gb300.serving import DdmServer, GpuExecutor, Request, latency_summary, replay
+
+    _build.build()
+    device = torch.device("cuda", 0)
+    n_req = args.requests
+    rng = np.random.default_rng(7)
+    scenes = synthetic.config4_scenes(n_req, seed=100)
+    big = rng.random(n_req) < 0.05
+    scenes = [synthetic.Scene(2000, 1024, 1024, 1024 * 1024 // 82, 2.0, 2000.0, 0.5, 500.0, 0.0, "uint16", 900 + i)
+              if big[i] else sc for i, sc in enumerate(scenes)]
+    arrivals = np.cumsum(rng.exponential(1.0 / 50.0, n_req))
+    frames = [synthetic.make_stack_torch(sc, device=device) for sc in scenes]
+    torch.cuda.synchronize(device)
+    total_frames = sum(sc.length for sc in scenes)
+
+    def requests():
+        return [Request(i, frames[i], np.arange(1, scenes[i].length), "fft", None, float(arrivals[i]))
+                for i in range(n_req)]
+
+    results = {}
+    for label, prec, streams in (("continuous_batching", args.precision, 6), ("one_at_a_time_f64", "f64", 1)):
+        torch.cuda.empty_cache()
+        free, _ = torch.cuda.mem_get_info(device)
+        ex = GpuExecutor(0, prec, streams)
+        server = DdmServer(ex, int(0.85 * free))
+        # warm-up: FFT tables of every frame size and every temporal length in the stream
+        for side in sorted({sc.height for sc in scenes}):
+            p = DdmPlan("fft", 8, side, side, 2, np.arange(1, 8), side, side, 16, False, prec, device)
+            f = torch.zeros((8, side, side), dtype=frames[0].dtype, device=device)
+            p.run(f, None, torch.empty(p.out_shape, dtype=torch.float64, device=device))
+        for T in sorted({sc.length for sc in scenes}):
+            p = DdmPlan("fft", T, 2, 2, 2, np.arange(1, T), 2, 2, 2 * T, False, prec, device)
+            f = torch.zeros((T, 2, 2), dtype=frames[0].dtype, device=device)
+            p.run(f, None, torch.empty(p.out_shape, dtype=torch.float64, device=device))
+        torch.cuda.synchronize(device)
+        ex.clock_start()
+        reqs = replay(server, requests(), time.perf_counter)
+        span = max(r.completed for r in reqs) - min(r.arrival for r in reqs)
+        summ = latency_summary(reqs)
+        summ.update({"frames_per_s": total_frames / span, "span_s": span, "peak_inflight": server.peak_inflight})
+        results[label] = summ
+        if label == "continuous_batching":
+            # a few results again, each alone on an idle device: must be identical
+            same = True
+            for i in list(range(0, n_req, max(1, n_req // 8)))[:8]:
+                sc = scenes[i]
+                p = DdmPlan("fft", sc.length, sc.height, sc.width, 2, np.arange(1, sc.length), sc.width, sc.height,
+                            2 * sc.length, False, prec, device)
+                alone = torch.empty(p.out_shape, dtype=torch.float64, device=device)
+                p.run(frames[i], None, alone)
+                torch.cuda.synchronize(device)
+                mixed = server.finished[i].result
+                same = same and bool(torch.equal(alone, mixed))
+                del p, alone
+            results[label]["identical_alone_and_in_mix"] = same
+        del server, ex, reqs
+    cb = results["continuous_batching"]
+    line = {
+        "metric": "serve p50/p99 latency", "value": cb["p99_ms"], "unit": "ms (p99)", "n_gpus": 1,
+        "higher_is_better": False, "dtype": args.precision, "data": "synthetic",
+        "config": {"workload": f"serve_{n_req}_requests_poisson_50_per_s", "requests": n_req,
+                   "large_jobs": int(big.sum()), "frames": total_frames, "mode": "fft"},
+        "serve": results,
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -464,9 +603,14 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--validate", action="store_true", help="report sampled errors against exact FP64 spectra")
+    ap.add_argument("--requests", type=int, default=100, help="serve: number of requests")
     args = ap.parse_args()
     if args.validate:
         run_validate(args)
+    elif args.config == "batch":
+        run_batch(args)
+    elif args.config == "serve":
+        run_serve(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -34,6 +34,26 @@ DTYPE_CODE = {
     "float64": 8,
 }
 
+class Job(ctypes.Structure):
+    """``fddm_b200_job`` of include/fddm_b200.h."""
+
+    _fields_ = [
+        ("mode", ctypes.c_int),
+        ("d_img_seq", ctypes.c_void_p),
+        ("dtype", ctypes.c_int),
+        ("length", ctypes.c_uint64),
+        ("height", ctypes.c_uint64),
+        ("width", ctypes.c_uint64),
+        ("lags", ctypes.POINTER(ctypes.c_uint32)),
+        ("nlags", ctypes.c_uint64),
+        ("nx", ctypes.c_uint64),
+        ("ny", ctypes.c_uint64),
+        ("nt", ctypes.c_uint64),
+        ("d_window", ctypes.c_void_p),
+        ("d_out", ctypes.c_void_p),
+    ]
+
+
 # every symbol the header declares, with (restype, argtypes)
 _u64 = ctypes.c_uint64
 _vp = ctypes.c_void_p
@@ -64,6 +84,12 @@ _SIGNATURES = {
         ctypes.c_int,
         [_vp, ctypes.c_int, _u64, _u64, _u64, ctypes.POINTER(ctypes.c_uint32), _u64, _u64, _u64, _u64,
          _vp, _vp, ctypes.c_int, _vp],
+    ),
+    "fddm_b200_batch_workspace_size": (
+        ctypes.c_int, [ctypes.POINTER(Job), ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]
+    ),
+    "fddm_b200_batch_run": (
+        ctypes.c_int, [ctypes.POINTER(Job), ctypes.c_uint64, ctypes.c_int, _vp, ctypes.c_size_t, _vp]
     ),
     "fddm_b200_set_stage_timing": (ctypes.c_int, [ctypes.c_int]),
     "fddm_b200_stage_times": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),

@@ -84,32 +84,48 @@ def make_stack_torch(scene: Scene, device="cuda", batch: int = 32, length: Optio
     g.manual_seed(scene.seed)
     T = scene.length if length is None else length
     H, W, S = scene.height, scene.width, scene.n_spots
-    f32 = torch.float32
-    x = torch.rand(S, generator=g, device=device, dtype=torch.float64) * W
-    y = torch.rand(S, generator=g, device=device, dtype=torch.float64) * H
+    f64 = torch.float64
+    x0 = torch.rand(S, generator=g, device=device, dtype=f64) * W
+    y0 = torch.rand(S, generator=g, device=device, dtype=f64) * H
     step = float(np.sqrt(2.0 * scene.diffusivity))
     tdtype = {"uint8": torch.uint8, "uint16": getattr(torch, "uint16", torch.int32), "int16": torch.int16}[scene.dtype]
     hi = float(np.iinfo(scene.dtype).max)
     out = torch.empty((T, H, W), dtype=tdtype, device=device)
-    gxs = torch.arange(W, device=device, dtype=torch.float64)
-    gys = torch.arange(H, device=device, dtype=torch.float64)
+    gxs = torch.arange(W, device=device, dtype=f64)
+    gys = torch.arange(H, device=device, dtype=f64)
 
     def prof(pos, grid, n):
         d = grid[None, None, :] - pos[:, :, None]
         d = d - n * torch.round(d / n)
-        return torch.exp(-(d * d) / (2.0 * scene.sigma ** 2)).to(f32)
+        return torch.exp(-(d * d) / (2.0 * scene.sigma ** 2)).to(torch.float32)
 
     for t0 in range(0, T, batch):
         nb = min(batch, T - t0)
-        xs = torch.empty((nb, S), device=device, dtype=torch.float64)
-        ys = torch.empty((nb, S), device=device, dtype=torch.float64)
-        for i in range(nb):
-            xs[i], ys[i] = x, y
-            x = torch.remainder(x + torch.randn(S, generator=g, device=device, dtype=torch.float64) * step + scene.drift, W)
-            y = torch.remainder(y + torch.randn(S, generator=g, device=device, dtype=torch.float64) * step + scene.drift, H)
-        gx = prof(xs, gxs, W)  # (nb, S, W)
-        gy = prof(ys, gys, H)  # (nb, S, H)
-        inten = scene.offset + scene.amplitude * torch.bmm(gy.transpose(1, 2), gx)
+        # Brownian steps with drift; frame i of the batch sits after i steps
+        sx = torch.randn((nb, S), generator=g, device=device, dtype=f64) * step + scene.drift
+        sy = torch.randn((nb, S), generator=g, device=device, dtype=f64) * step + scene.drift
+        cx = torch.cumsum(sx, dim=0)
+        cy = torch.cumsum(sy, dim=0)
+        xs = torch.remainder(x0[None] + torch.cat([torch.zeros_like(cx[:1]), cx[:-1]]), W)
+        ys = torch.remainder(y0[None] + torch.cat([torch.zeros_like(cy[:1]), cy[:-1]]), H)
+        x0 = torch.remainder(x0 + cx[-1], W)
+        y0 = torch.remainder(y0 + cy[-1], H)
+        inten = scene.offset + scene.amplitude * torch.bmm(prof(ys, gys, H).transpose(1, 2), prof(xs, gxs, W))
         frame = torch.poisson(inten, generator=g).clamp_(0, hi)
         out[t0:t0 + nb] = frame.to(torch.int32).to(tdtype)
+    return out
+
+
+def config4_scenes(n_stacks: int = 96, seed: int = 0):
+    """Uneven ROI stacks: side from {64, 96, 128, 192, 256, 384, 512}, T uniform in [100, 2000],
+    diffusivity log-uniform in [0.05, 2] px^2/frame, uint16, one spot per ~82 px^2
+    (the density of the 64-frame configuration), spot width 2 px, amplitude 2000 on 500."""
+    rng = np.random.default_rng(seed)
+    sides = [64, 96, 128, 192, 256, 384, 512]
+    out = []
+    for i in range(n_stacks):
+        side = int(rng.choice(sides))
+        T = int(rng.integers(100, 2001))
+        D = float(np.exp(rng.uniform(np.log(0.05), np.log(2.0))))
+        out.append(Scene(T, side, side, max(1, side * side // 82), 2.0, 2000.0, D, 500.0, 0.0, "uint16", seed + i))
     return out

@@ -116,6 +116,34 @@ int fddm_b200_ddm_from_host(int mode, const void* h_img_seq, int dtype, uint64_t
                             uint64_t nt, void* d_frames, const double* d_window, double* d_out, double* h_out,
                             void* d_workspace, size_t workspace_bytes, int precision, void* stream);
 
+/* Batched jobs: many independent stacks of uneven size, length and mode in
+   one call (the reference processes one stack per call; this replaces a
+   Python loop over ddm() for multi-ROI analysis).  Each job is the argument
+   list of fddm_b200_ddm_fft / _diff. */
+typedef struct fddm_b200_job {
+  int mode;                 /* FDDM_MODE_FFT or FDDM_MODE_DIFF */
+  const void* d_img_seq;    /* (length, height, width) device frames */
+  int dtype;                /* FDDM_U8 ... FDDM_F64 (64-bit integers excluded) */
+  uint64_t length, height, width;
+  const uint32_t* lags;     /* host, nlags entries */
+  uint64_t nlags;
+  uint64_t nx, ny, nt;      /* nt ignored in diff mode */
+  const double* d_window;   /* (height, width) or NULL */
+  double* d_out;            /* (nlags + 2, ny, nx/2 + 1) */
+} fddm_b200_job;
+
+/* Workspace bytes of fddm_b200_batch_run for these jobs (sum of the jobs' own
+   workspaces, 256-byte aligned). */
+int fddm_b200_batch_workspace_size(const fddm_b200_job* jobs, uint64_t njobs, int precision, size_t* bytes);
+
+/* Run all jobs.  Every job is validated before anything is launched; the jobs
+   are then scheduled longest-first onto library-owned streams forked from
+   `stream` and joined back into it, so the batch completes in stream order
+   while independent jobs overlap on the GPU.  Each job's result is identical
+   to running it alone. */
+int fddm_b200_batch_run(const fddm_b200_job* jobs, uint64_t njobs, int precision, void* d_workspace,
+                        size_t workspace_bytes, void* stream);
+
 /* Weighted azimuthal average of a stack of half-plane maps: the per-(bin, row)
    weighted mean and unbiased weighted standard deviation.  Replaces the two
    per-pixel loops of azimuthal_average_array (src/python/azimuthalaverage.py:435-444
