@@ -415,7 +415,7 @@ def run_validate(args):
     window = torch.from_numpy(wnp).to(device) if wnp is not None else None
     results = {}
     outs = {}
-    for mode, prec in (("fft", args.precision), ("diff", args.precision), ("fft", "f64")):
+    for mode, prec in (("fft", args.precision), ("diff", args.precision), ("fft", "f64"), ("fft", "f32")):
         plan = DdmPlan(mode, T, H, W, code, lags, nx, ny, nt if mode == "fft" else 0, window is not None, prec, device)
         out = torch.empty(plan.out_shape, dtype=torch.float64, device=device)
         plan.run(frames, window, out)
