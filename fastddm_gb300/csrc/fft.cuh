@@ -193,7 +193,7 @@ __device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int 
       dft<S, R, false>(v);
       if (j != 0) {
 #pragma unroll
-        for (int m = 1; m < R; ++m) v[m] = cmul(v[m], tw[twstep * j * m]);
+        for (int m = 1; m < R; ++m) v[m] = twmul<S>::mul(v[m], tw[twstep * j * m]);
       }
     } else {
       if (j != 0) {
@@ -243,7 +243,7 @@ __device__ __forceinline__ void fft_first_pass_padded(cx<S>* __restrict__ buf, c
     else dft<S, R, false>(v);
     if (j != 0) {
 #pragma unroll
-      for (int m = 1; m < R; ++m) v[m] = cmul(v[m], tw[j * m]);
+      for (int m = 1; m < R; ++m) v[m] = twmul<S>::mul(v[m], tw[j * m]);
     }
 #pragma unroll
     for (int r = 0; r < R; ++r) buf[swz<S>(j + r * stride)] = v[r];

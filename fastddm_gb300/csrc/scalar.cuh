@@ -167,6 +167,12 @@ template <class S> __device__ __forceinline__ cx<S> bsub(cx<S> a, cx<S> b) {
   return {bfly<S>::sub(a.r, b.r), bfly<S>::sub(a.i, b.i)};
 }
 
+// twiddle products inside FFT passes (float-float: not renormalised)
+template <class S> __device__ __forceinline__ cx<S> cmul(cx<S> a, cx<S> b);
+template <class S> struct twmul {
+  static __device__ __forceinline__ cx<S> mul(cx<S> a, cx<S> b) { return cmul(a, b); }
+};
+
 template <class S> __device__ __forceinline__ cx<S> cadd(cx<S> a, cx<S> b) {
   return {sc<S>::add(a.r, b.r), sc<S>::add(a.i, b.i)};
 }
@@ -197,12 +203,33 @@ __device__ __forceinline__ ff ff_dot2(ff a, ff b, ff c, ff d, float sgn) {  // a
   lo = __fmaf_rn(cl, d.h, lo);
   return fast_two_sum(s.h, lo);
 }
+// ff_dot2 without the final renormalisation (the pair is exact TwoSum of the
+// leading products plus the folded low-order terms); for twiddle products that
+// only feed further butterfly additions.
+__device__ __forceinline__ ff ff_dot2_nn(ff a, ff b, ff c, ff d, float sgn) {
+  const float p1 = __fmul_rn(a.h, b.h), e1 = __fmaf_rn(a.h, b.h, -p1);
+  const float ch = __fmul_rn(sgn, c.h), cl = __fmul_rn(sgn, c.l);
+  const float p2 = __fmul_rn(ch, d.h), e2 = __fmaf_rn(ch, d.h, -p2);
+  const ff s = two_sum(p1, p2);
+  float lo = __fadd_rn(__fadd_rn(e1, e2), s.l);
+  lo = __fmaf_rn(a.h, b.l, lo);
+  lo = __fmaf_rn(a.l, b.h, lo);
+  lo = __fmaf_rn(ch, d.l, lo);
+  lo = __fmaf_rn(cl, d.h, lo);
+  return {s.h, lo};
+}
 template <> __device__ __forceinline__ cx<ff> cmul<ff>(cx<ff> a, cx<ff> b) {
   return {ff_dot2(a.r, b.r, a.i, b.i, -1.0f), ff_dot2(a.r, b.i, a.i, b.r, 1.0f)};
 }
 template <> __device__ __forceinline__ cx<ff> cmulc<ff>(cx<ff> a, cx<ff> b) {
   return {ff_dot2(a.r, b.r, a.i, b.i, 1.0f), ff_dot2(a.i, b.r, a.r, b.i, -1.0f)};
 }
+
+template <> struct twmul<ff> {
+  static __device__ __forceinline__ cx<ff> mul(cx<ff> a, cx<ff> b) {
+    return {ff_dot2_nn(a.r, b.r, a.i, b.i, -1.0f), ff_dot2_nn(a.r, b.i, a.i, b.r, 1.0f)};
+  }
+};
 
 template <class S> __device__ __forceinline__ cx<S> cscale(cx<S> a, S s) {
   return {sc<S>::mul(a.r, s), sc<S>::mul(a.i, s)};
