@@ -360,25 +360,56 @@ template <> struct cvt<double, double> {
 //   lags need
 //   X = FFT_N(G zero-padded), P = |X|^2 (real)
 //   Re C(lag) = (1/N) Re DFT_N(P)(lag) (cos is even, so the forward transform
-//   serves), evaluated through one half-length complex FFT of
+//   serves), evaluated through one half-length complex transform of
 //   z[m] = P(2m) + i P(2m+1) and a per-lag post-process, only at the lags
 //   D(lag) = (S1 + S2 - 2 Re C) / (T - lag)
 // Lags with T - lag <= kDirect are summed directly from the saved first and
 // last kDirect values of G: there the Wiener-Khinchin form would amplify its
 // rounding error by T / (T - lag).
-// Shared memory (see temporal_smem): buf (N), z (N/2), head, tail (kDirect
-// each), reduction scratch, the lag slot tables (int16, loaded once per CTA)
-// and, when they fit, the needed prefix sums (else per-CTA global scratch).
+//
+// The length-N forward FFT leaves X(k) at the digit-reversed position
+// p(k) = m_0 M_1 + r with m_0 = k mod R_0 and r fixed by the higher digits.
+// For even R_0, P(2m) and P(2m+1) sit at (2a) M_1 + r and (2a+1) M_1 + r, and
+// a M_1 + r is exactly where the half-length plan (R_0/2, R_1, ...) keeps
+// element m in its own digit-reversed order.  So conj(z) is formed in place
+// without any permutation table, and the inverse passes of the half plan
+// (digit-reversed in, natural out) give Y = conj(DFT_{N/2}(z)) in natural order.
+//
+// Shared memory (temporal_fft_smem): buf (the larger of N and
+// swz_round(N/2) + swz_round(T) elements; the next mode's series is prefetched
+// to buf + swz_round(N/2) while the half-length transform runs below it),
+// head, tail (kDirect each), reduction scratch, the lag slot tables (int16,
+// loaded once per CTA) and, when they fit, the needed prefix sums (else
+// per-CTA global scratch).
 // ---------------------------------------------------------------------------
 constexpr int kDirect = 32;
+
+// P = |X|^2 of one length-N forward transform, paired in place as
+// conj(z[m]) = P(2m) - i P(2m+1) at the half plan's position a M_1 + r.  A
+// thread owns the R0 positions j M_1 + r of its r: it reads all of them
+// before writing, and no other thread touches them.
+template <class S, int R0>
+__device__ __forceinline__ void pair_power(cx<S>* __restrict__ buf, int M1, int tid, int nthr) {
+  for (int r = tid; r < M1; r += nthr) {
+    S pw[R0];
+#pragma unroll
+    for (int j = 0; j < R0; ++j) {
+      const cx<S> x = buf[swz<S>(j * M1 + r)];
+      pw[j] = sc<S>::sqsum(x.r, x.i);
+    }
+#pragma unroll
+    for (int h = 0; h < R0 / 2; ++h) buf[swz<S>(h * M1 + r)] = {pw[2 * h], sc<S>::neg(pw[2 * h + 1])};
+  }
+}
 
 template <class S, class A>
 __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int T = a.T, N = a.nt, N2 = a.nt / 2, nl = a.nlags;
   cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
-  cx<S>* z = buf + swz_round<S>(N);
-  cx<S>* head = z + swz_round<S>(N2);
+  const int up = swz_round<S>(N2);
+  cx<S>* ser = buf + up;  // the prefetched series of the next mode
+  cx<S>* head = buf + max(swz_round<S>(N), up + swz_round<S>(T));
   cx<S>* tail = head + kDirect;
   A* scratch = reinterpret_cast<A*>(tail + kDirect);
   short* slotA = reinterpret_cast<short*>(scratch + 96);
@@ -391,27 +422,25 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
   const cx<S>* F = reinterpret_cast<const cx<S>*>(a.spec);
   const cx<S>* tw = reinterpret_cast<const cx<S>*>(a.twt);
   const cx<S>* tw2 = reinterpret_cast<const cx<S>*>(a.twt2);
-  const int* iperm = a.ipermt;
-  const int* perm2 = a.permt2;
   const A invT = sc<A>::cst(a.invT_h, a.invT_l, a.invT_d);
   const A invN = sc<A>::cst(a.invnt_h, a.invnt_l, a.invnt_d);
   const int chunk = (T + nthr - 1) / nthr;
   const int tail0 = T - kDirect;  // first index kept in `tail` (may be negative)
+  const int R0 = a.pt.radix[0], M1 = N / R0;
 
   for (int t = tid; t <= T; t += nthr) {
     slotA[t] = (short)a.slotA[t];
     slotB[t] = (short)a.slotB[t];
   }
-  if (blockIdx.x < a.Q) prefetch_series<S>(buf, F + (size_t)blockIdx.x * a.Tpad, T, tid, nthr);
+  if (blockIdx.x < a.Q) prefetch_series<S>(ser, F + (size_t)blockIdx.x * a.Tpad, T, tid, nthr);
 
   for (size_t q = blockIdx.x; q < a.Q; q += gridDim.x) {
-    // this mode's series was prefetched into buf[0, T); buf[T, N) is never read
     cp_async_wait_all();
     __syncthreads();
 
     A v[3] = {sc<A>::zero(), sc<A>::zero(), sc<A>::zero()};
     for (int t = tid; t < T; t += nthr) {
-      const cx<S> f = buf[swz<S>(t)];
+      const cx<S> f = ser[swz<S>(t)];
       const A fr = cvt<S, A>::to_acc(f.r), fi = cvt<S, A>::to_acc(f.i);
       v[0] = sc<A>::add(v[0], fr);
       v[1] = sc<A>::add(v[1], fi);
@@ -422,11 +451,11 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
     const A ps = sc<A>::mul(v[2], invT);
     const S msr = cvt<S, A>::to_fft(mr), msi = cvt<S, A>::to_fft(mi);
 
-    // G = F - <F>; |G|^2 summed over a contiguous chunk per thread
+    // G = F - <F> into buf[0, T); |G|^2 summed over a contiguous chunk per thread
     const int t_beg = min(T, tid * chunk), t_end = min(T, t_beg + chunk);
     A run = sc<A>::zero();
     for (int t = t_beg; t < t_end; ++t) {
-      cx<S> g = buf[swz<S>(t)];
+      cx<S> g = ser[swz<S>(t)];
       g.r = sc<S>::sub(g.r, msr);
       g.i = sc<S>::sub(g.i, msi);
       buf[swz<S>(t)] = g;
@@ -448,29 +477,24 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
     __syncthreads();
 
     fft_forward_padded<S>(buf, a.pt, T, tw, tid, nthr);
-    // P(k) = |X(k)|^2 scattered into z as the real sequence z[k/2].{r,i}
-    for (int p = tid; p < N; p += nthr) {
-      const cx<S> x = buf[swz<S>(p)];
-      const int k = iperm[p];
-      const S pv = sc<S>::sqsum(x.r, x.i);
-      cx<S>* e = &z[swz<S>(k >> 1)];
-      if (k & 1) e->i = pv;
-      else e->r = pv;
-    }
+    if (R0 == 8) pair_power<S, 8>(buf, M1, tid, nthr);
+    else if (R0 == 4) pair_power<S, 4>(buf, M1, tid, nthr);
+    else pair_power<S, 2>(buf, M1, tid, nthr);
     __syncthreads();
-    // buf is free until the next iteration: start loading the next mode
-    if (q + gridDim.x < a.Q) prefetch_series<S>(buf, F + (q + gridDim.x) * a.Tpad, T, tid, nthr);
-    fft_forward<S>(z, 1, N2, a.pt2, tw2, tid, nthr);
+    // buf above the half-length transform is free: start loading the next mode
+    if (q + gridDim.x < a.Q) prefetch_series<S>(ser, F + (q + gridDim.x) * a.Tpad, T, tid, nthr);
+    fft_inverse<S>(buf, 1, N2, a.pt2, tw2, tid, nthr);
 
     for (int l = tid; l < nl; l += nthr) {
       const int tau = a.lags[l];
       if (T - tau <= kDirect) continue;
-      const cx<S> zk = z[swz<S>(perm2[tau])];
-      const cx<S> zn = z[swz<S>(perm2[tau == 0 ? 0 : N2 - tau])];
+      // Y = conj(Z), Z = DFT_{N/2}(z), in natural order
+      const cx<S> yk = buf[swz<S>(tau)];
+      const cx<S> yn = buf[swz<S>(tau == 0 ? 0 : N2 - tau)];
       // DFT_N(P)(tau) = Xe + w^tau Xo with Xe = (Zk + conj Zn)/2, Xo = (Zk - conj Zn)/(2i);
       // y is twice its real part
-      const S xe = sc<S>::add(zk.r, zn.r);
-      const cx<S> xo = {sc<S>::add(zk.i, zn.i), sc<S>::sub(zn.r, zk.r)};
+      const S xe = sc<S>::add(yk.r, yn.r);
+      const cx<S> xo = {sc<S>::neg(sc<S>::add(yk.i, yn.i)), sc<S>::sub(yn.r, yk.r)};
       const cx<S> w = tw[tau];
       const S y = sc<S>::add(xe, sc<S>::sub(sc<S>::mul(w.r, xo.r), sc<S>::mul(w.i, xo.i)));
       // 2 Re C = y / N

@@ -221,8 +221,11 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   size_t smem_t = (size_t)T * sizeof(cx<S>) + 96 * sizeof(A);
   int threads = temporal_threads(T);
   if (r.mode == MODE_FFT) {
-    ta.pt = tt.plan; ta.twt = tt.tw; ta.ipermt = tt.iperm;
-    ta.pt2 = tt2.plan; ta.twt2 = tt2.tw; ta.permt2 = tt2.perm;
+    ta.twt = tt.tw; ta.twt2 = tt2.tw;
+    if (!temporal_plan(N, ta.pt) || !half_plan(ta.pt, ta.pt2)) {
+      err = "no temporal plan for length " + std::to_string(N);
+      return 4;
+    }
     ta.slotA = d_slots; ta.slotB = d_slots + (T + 1);
     ta.need = ws + L.need_off;
     const size_t with_need = temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), true);

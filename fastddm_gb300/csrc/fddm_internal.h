@@ -43,11 +43,9 @@ struct TemporalArgs {
   const void* spec;
   size_t Q;
   int Tpad, T, nt, nlags;  // nt: the temporal transform length N chosen by plan_layout
-  FftPlan pt, pt2;         // plans for N and N/2
-  const void* twt;
-  const void* twt2;
-  const int* ipermt;      // position -> natural index after the length-N forward FFT
-  const int* permt2;      // natural index -> position after the length-N/2 forward FFT
+  FftPlan pt, pt2;         // plan for N and the half-length plan derived from it (half_plan)
+  const void* twt;         // twiddles of length N
+  const void* twt2;        // twiddles of length N/2
   const int* slotA;      // (T + 1): lag index l with T - lag_l == t, or -1
   const int* slotB;      // (T + 1): lag index l with lag_l == t, or -1
   void* need;            // per-CTA scratch, (2 * nlags + 2) accumulators per CTA
@@ -138,6 +136,13 @@ size_t spec_elem_bytes(int precision);
 bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err);
 // Factor n into supported radices; false if n has another prime factor.
 bool make_plan(int n, FftPlan& p);
+// Plan of length n/2 whose digit-reversed order matches the even outputs of
+// p: radices (R_0/2, R_1, ...), the first dropped when R_0 = 2.  Requires an
+// even n and an even R_0 (make_plan puts the radices 8, 4, 2 first).
+bool half_plan(const FftPlan& p, FftPlan& h);
+// Plan of the length-n temporal transform (n even): the even first radix that
+// makes the padded first pass and the half-length transform cheapest.
+bool temporal_plan(int n, FftPlan& p);
 
 // Per-precision pipeline entry points (instantiated in ddm_ff.cu, ddm_f64.cu, ddm_f32.cu).
 int run_ddm_ff(const DdmRequest& r, cudaStream_t st, std::string& err);

@@ -169,8 +169,10 @@ template <class S> __device__ __forceinline__ cx<S> bsub(cx<S> a, cx<S> b) {
 
 // twiddle products inside FFT passes (float-float: not renormalised)
 template <class S> __device__ __forceinline__ cx<S> cmul(cx<S> a, cx<S> b);
+template <class S> __device__ __forceinline__ cx<S> cmulc(cx<S> a, cx<S> b);
 template <class S> struct twmul {
   static __device__ __forceinline__ cx<S> mul(cx<S> a, cx<S> b) { return cmul(a, b); }
+  static __device__ __forceinline__ cx<S> mulc(cx<S> a, cx<S> b) { return cmulc(a, b); }  // a * conj(b)
 };
 
 template <class S> __device__ __forceinline__ cx<S> cadd(cx<S> a, cx<S> b) {
@@ -228,6 +230,9 @@ template <> __device__ __forceinline__ cx<ff> cmulc<ff>(cx<ff> a, cx<ff> b) {
 template <> struct twmul<ff> {
   static __device__ __forceinline__ cx<ff> mul(cx<ff> a, cx<ff> b) {
     return {ff_dot2_nn(a.r, b.r, a.i, b.i, -1.0f), ff_dot2_nn(a.r, b.i, a.i, b.r, 1.0f)};
+  }
+  static __device__ __forceinline__ cx<ff> mulc(cx<ff> a, cx<ff> b) {
+    return {ff_dot2_nn(a.r, b.r, a.i, b.i, 1.0f), ff_dot2_nn(a.i, b.r, a.r, b.i, -1.0f)};
   }
 };
 

@@ -9,6 +9,24 @@
 
 namespace fddm {
 
+// Block sizes and shift tables of a plan whose n and radices are set.
+static void finish_plan(FftPlan& p) {
+  auto lg = [](int v) -> int {
+    if (v <= 0 || (v & (v - 1))) return -1;
+    int l = 0;
+    while ((1 << l) < v) ++l;
+    return l;
+  };
+  p.lgn = lg(p.n);
+  int M = p.n;
+  for (int s = 0; s < p.npass; ++s) {
+    p.block[s] = M;
+    p.lgstride[s] = lg(M / p.radix[s]);
+    p.lgbpf[s] = lg(p.n / p.radix[s]);
+    M /= p.radix[s];
+  }
+}
+
 bool make_plan(int n, FftPlan& p) {
   if (n < 1) return false;
   p.n = n;
@@ -27,20 +45,17 @@ bool make_plan(int n, FftPlan& p) {
   for (int r : odd)
     while (m % r == 0) if (!push(r)) return false;
   if (m != 1) return false;
-  auto lg = [](int v) -> int {
-    if (v <= 0 || (v & (v - 1))) return -1;
-    int l = 0;
-    while ((1 << l) < v) ++l;
-    return l;
-  };
-  p.lgn = lg(n);
-  int M = n;
-  for (int s = 0; s < p.npass; ++s) {
-    p.block[s] = M;
-    p.lgstride[s] = lg(M / p.radix[s]);
-    p.lgbpf[s] = lg(n / p.radix[s]);
-    M /= p.radix[s];
-  }
+  finish_plan(p);
+  return true;
+}
+
+bool half_plan(const FftPlan& p, FftPlan& h) {
+  if (p.npass < 1 || p.n % 2 || p.radix[0] % 2) return false;
+  h.n = p.n / 2;
+  h.npass = 0;
+  if (p.radix[0] > 2) h.radix[h.npass++] = p.radix[0] / 2;
+  for (int s = 1; s < p.npass; ++s) h.radix[h.npass++] = p.radix[s];
+  finish_plan(h);
   return true;
 }
 
@@ -167,25 +182,55 @@ static double pass_cost(int r) {
   }
 }
 
-static double fft_cost(int n) {
-  FftPlan p;
-  if (!make_plan(n, p)) return 1e300;
-  double c = 0.0;
-  for (int s = 0; s < p.npass; ++s) c += pass_cost(p.radix[s]);
-  return c * n;
+// First pass of a zero-padded input: the upper half of every butterfly is
+// zero (the add/sub stage of radix 8 and 4 halves, radix 2 is twiddles only).
+static double padded_cost(int r) {
+  switch (r) {
+    case 8: return 95.0;
+    case 4: return 55.0;
+    case 2: return 25.0;
+    default: return pass_cost(r);
+  }
 }
+
+// Cheapest plan of the temporal transforms for length n: the first radix
+// (even, run as the padded pass) is chosen by cost, the others follow
+// make_plan's order; the half-length transform uses half_plan of it.
+static double temporal_plan_cost(int n, FftPlan* out) {
+  double best = 1e300;
+  for (int r0 : {8, 4, 2}) {
+    if (n % r0) continue;
+    FftPlan rest, cand, h;
+    if (!make_plan(n / r0, rest) || rest.npass + 1 > kMaxPass) continue;
+    cand.n = n;
+    cand.npass = 0;
+    cand.radix[cand.npass++] = r0;
+    for (int s = 0; s < rest.npass; ++s) cand.radix[cand.npass++] = rest.radix[s];
+    finish_plan(cand);
+    if (!half_plan(cand, h)) continue;
+    double c = padded_cost(r0) * n;
+    for (int s = 1; s < cand.npass; ++s) c += pass_cost(cand.radix[s]) * n;
+    for (int s = 0; s < h.npass; ++s) c += pass_cost(h.radix[s]) * h.n;
+    if (c < best) {
+      best = c;
+      if (out) *out = cand;
+    }
+  }
+  return best;
+}
+static double temporal_cost(int n) { return temporal_plan_cost(n, nullptr); }
+
+bool temporal_plan(int n, FftPlan& p) { return temporal_plan_cost(n, &p) < 1e300; }
 
 int choose_temporal_length(int64_t T) {
   const int64_t lo = std::max<int64_t>(2, 2 * T - 1);
   int64_t p2 = 1;
   while (p2 < lo) p2 <<= 1;
   int best = (int)p2;
-  double best_cost = fft_cost(best) + fft_cost(best / 2);
+  double best_cost = temporal_cost(best);
   for (int64_t n = lo; n < p2; ++n) {
     if (n % 2) continue;
-    FftPlan p;
-    if (!make_plan((int)n, p)) continue;
-    const double c = fft_cost((int)n) + fft_cost((int)(n / 2));
+    const double c = temporal_cost((int)n);
     if (c < best_cost) {
       best_cost = c;
       best = (int)n;
@@ -198,7 +243,10 @@ static size_t round_to(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 size_t temporal_fft_smem(int T, int N, int nlags, size_t es, size_t ea, bool need_in_smem) {
   const size_t g = 128 / es;  // swizzle group (elements)
-  size_t b = (round_to(N, g) + round_to(N / 2, g) + 64) * es + 96 * ea + 2 * (size_t)(T + 1) * sizeof(short);
+  // transform buffer: the length-N transform, or the half-length transform
+  // below the next series prefetched from offset round_to(N / 2, g)
+  const size_t nbuf = std::max(round_to(N, g), round_to(N / 2, g) + round_to(T, g));
+  size_t b = (nbuf + 64) * es + 96 * ea + 2 * (size_t)(T + 1) * sizeof(short);
   if (need_in_smem) b = round_to(b, 16) + (2 * (size_t)nlags + 2) * ea;
   return b;
 }
