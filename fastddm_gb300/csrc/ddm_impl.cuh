@@ -71,6 +71,13 @@ template <> __device__ __forceinline__ ff shfl_up<ff>(ff v, int o) {
 template <> __device__ __forceinline__ double shfl_up<double>(double v, int o) {
   return __shfl_up_sync(0xffffffffu, v, o);
 }
+template <class A> __device__ __forceinline__ A shfl_idx(A v, int src);
+template <> __device__ __forceinline__ ff shfl_idx<ff>(ff v, int src) {
+  return {__shfl_sync(0xffffffffu, v.h, src), __shfl_sync(0xffffffffu, v.l, src)};
+}
+template <> __device__ __forceinline__ double shfl_idx<double>(double v, int src) {
+  return __shfl_sync(0xffffffffu, v, src);
+}
 
 template <class A> __device__ __forceinline__ A warp_sum(A v) {
 #pragma unroll
@@ -527,15 +534,249 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Stage 3 (diff mode)
-// dynamic smem: T * cx<S> + 96 * A
+// Stage 3 (fft mode) for series whose length-N transform does not fit in
+// shared memory.  N = R0 M1 (R0 in {2, 4, 8}): the first DIF pass runs from
+// the spectrum into the CTA's global scratch X, the length-M1 sub-transforms
+// run in shared memory.  Per q:
+//   A  mean and PS from coalesced sums
+//   B  G = F - <F>: warp-segmented inclusive prefix sums of |G|^2 into the
+//      global scratch, the first and last kDirect values of G into shared memory
+//   C  first pass (radix R0, zero-padded input read from the spectrum) into
+//      X[m M1 + j]
+//   D  for h < R0/2: sub-blocks 2h and 2h+1 through the remaining forward
+//      passes, paired into conj(z) exactly as pair_power does, through the
+//      inverse passes of the half plan below its first pass, and stored to
+//      X[h M1 + r] (region h was read in this or an earlier iteration)
+//   E  the half plan's first inverse pass (radix R0/2, stride M1) evaluated
+//      only at the outputs the lags need
+//   F  D(lag) as in k_tfft
+// dynamic smem (temporal_long_smem): swz_round(M1) cx<S> + M1 S (16-byte
+// aligned) + 2 kDirect cx<S> + 160 A
 // ---------------------------------------------------------------------------
+template <class S, int R0>
+__device__ __forceinline__ void long_first_pass(const cx<S>* __restrict__ src, cx<S>* __restrict__ X, int T, int M1,
+                                                S msr, S msi, const cx<S>* __restrict__ tw, int tid, int nthr) {
+  for (int j = tid; j < M1; j += nthr) {
+    cx<S> v[R0];
+#pragma unroll
+    for (int r = 0; r < R0; ++r) {
+      const int t = j + r * M1;
+      if (r < R0 / 2 && t < T) {
+        const cx<S> f = src[t];
+        v[r] = {sc<S>::sub(f.r, msr), sc<S>::sub(f.i, msi)};
+      } else {
+        v[r] = czero<S>();
+      }
+    }
+    dft_halfzero<S, R0>(v);
+    if (j != 0) {
+#pragma unroll
+      for (int m = 1; m < R0; ++m) v[m] = twmul<S>::mul(v[m], tw[j * m]);
+    }
+#pragma unroll
+    for (int m = 0; m < R0; ++m) X[j + m * M1] = v[m];
+  }
+}
+
+// v * i^e
+template <class S> __device__ __forceinline__ cx<S> mul_ipow(cx<S> v, int e) {
+  switch (e & 3) {
+    case 0: return v;
+    case 1: return {sc<S>::neg(v.i), v.r};
+    case 2: return {sc<S>::neg(v.r), sc<S>::neg(v.i)};
+    default: return {v.i, sc<S>::neg(v.r)};
+  }
+}
+
+// Output k of the half plan's first inverse pass (radix R, stride M1, length
+// R M1) from its input Z; twiddles w_{R M1}^{j r} = w_N^{2 j r}.
+template <class S, int R>
+__device__ __forceinline__ cx<S> half_first_inverse_at(const cx<S>* Z, int k, int M1, const cx<S>* twN) {
+  const int j = k % M1, m = k / M1;
+  cx<S> y = Z[j];
+#pragma unroll
+  for (int r = 1; r < R; ++r) {
+    cx<S> v = Z[j + r * M1];
+    if (j != 0) v = twmul<S>::mulc(v, twN[2 * j * r]);
+    y = cadd(y, mul_ipow(v, r * m * (4 / R)));  // w_R^(-r m) = i^(4 r m / R)
+  }
+  return y;
+}
+
 template <class S, class A>
+__global__ void __launch_bounds__(512) k_tfft_long(TemporalArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int T = a.T, N2 = a.nt / 2, nl = a.nlags, M1 = a.M1, R0 = a.R0;
+  cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
+  S* pe = reinterpret_cast<S*>(buf + swz_round<S>(M1));
+  cx<S>* head = reinterpret_cast<cx<S>*>(smem_raw + (((reinterpret_cast<unsigned char*>(pe + M1) - smem_raw) + 15) & ~15));
+  cx<S>* tail = head + kDirect;
+  A* scratch = reinterpret_cast<A*>(tail + kDirect);
+  A* woff = scratch + 96;  // exclusive prefix of the warp segments' totals, then the total
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
+  const cx<S>* F = reinterpret_cast<const cx<S>*>(a.spec);
+  const cx<S>* tw = reinterpret_cast<const cx<S>*>(a.twt);
+  const cx<S>* twm = reinterpret_cast<const cx<S>*>(a.twm);
+  unsigned char* xs = static_cast<unsigned char*>(a.xs) + (size_t)blockIdx.x * a.xs_stride;
+  cx<S>* X = reinterpret_cast<cx<S>*>(xs);
+  A* P = reinterpret_cast<A*>(xs + a.xs_pfx_off);
+  const A invT = sc<A>::cst(a.invT_h, a.invT_l, a.invT_d);
+  const A invN = sc<A>::cst(a.invnt_h, a.invnt_l, a.invnt_d);
+  const int tail0 = T - kDirect;
+  const int seg = ((T + nw - 1) / nw + 31) / 32 * 32;  // warp segment of the prefix sums
+
+  for (size_t q = blockIdx.x; q < a.Q; q += gridDim.x) {
+    const cx<S>* src = F + q * a.Tpad;
+    // A
+    A v[3] = {sc<A>::zero(), sc<A>::zero(), sc<A>::zero()};
+    for (int t = tid; t < T; t += nthr) {
+      const cx<S> f = src[t];
+      const A fr = cvt<S, A>::to_acc(f.r), fi = cvt<S, A>::to_acc(f.i);
+      v[0] = sc<A>::add(v[0], fr);
+      v[1] = sc<A>::add(v[1], fi);
+      v[2] = sc<A>::add(v[2], sc<A>::sqsum(fr, fi));
+    }
+    block_sum<A, 3>(v, scratch);
+    const A mr = sc<A>::mul(v[0], invT), mi = sc<A>::mul(v[1], invT);
+    const A ps = sc<A>::mul(v[2], invT);
+    const S msr = cvt<S, A>::to_fft(mr), msi = cvt<S, A>::to_fft(mi);
+
+    // B
+    {
+      const int s0 = warp * seg, s1 = min(T, s0 + seg);
+      A carry = sc<A>::zero();
+      for (int t0 = s0; t0 < s1; t0 += 32) {
+        const int t = t0 + lane;
+        A e = sc<A>::zero();
+        if (t < s1) {
+          cx<S> g = src[t];
+          g.r = sc<S>::sub(g.r, msr);
+          g.i = sc<S>::sub(g.i, msi);
+          if (t < kDirect) head[t] = g;
+          if (t >= tail0) tail[t - tail0] = g;
+          e = sc<A>::sqsum(cvt<S, A>::to_acc(g.r), cvt<S, A>::to_acc(g.i));
+        }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const A u = shfl_up(e, o);
+          if (lane >= o) e = sc<A>::add(e, u);
+        }
+        const A inc = sc<A>::add(carry, e);
+        if (t < s1) P[t] = inc;
+        carry = shfl_idx(inc, 31);
+      }
+      if (lane == 0) scratch[warp] = carry;
+      __syncthreads();
+      if (warp == 0) {
+        const A w = lane < nw ? scratch[lane] : sc<A>::zero();
+        A wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const A u = shfl_up(wi, o);
+          if (lane >= o) wi = sc<A>::add(wi, u);
+        }
+        woff[lane] = sc<A>::sub(wi, w);
+        if (lane == 31) woff[32] = wi;
+      }
+    }
+
+    // C (the spectrum is read again; X is free since the last iteration ended)
+    if (R0 == 8) long_first_pass<S, 8>(src, X, T, M1, msr, msi, tw, tid, nthr);
+    else if (R0 == 4) long_first_pass<S, 4>(src, X, T, M1, msr, msi, tw, tid, nthr);
+    else long_first_pass<S, 2>(src, X, T, M1, msr, msi, tw, tid, nthr);
+    __syncthreads();
+
+    // D
+    for (int h = 0; h < R0 / 2; ++h) {
+      const cx<S>* xe = X + (size_t)(2 * h) * M1;
+      for (int u = tid; u < M1; u += nthr) buf[swz<S>(u)] = xe[u];
+      __syncthreads();
+      fft_forward<S>(buf, 1, M1, a.pm, twm, tid, nthr);
+      for (int u = tid; u < M1; u += nthr) {
+        const cx<S> x = buf[swz<S>(u)];
+        pe[u] = sc<S>::sqsum(x.r, x.i);
+      }
+      __syncthreads();
+      const cx<S>* xo = X + (size_t)(2 * h + 1) * M1;
+      for (int u = tid; u < M1; u += nthr) buf[swz<S>(u)] = xo[u];
+      __syncthreads();
+      fft_forward<S>(buf, 1, M1, a.pm, twm, tid, nthr);
+      for (int u = tid; u < M1; u += nthr) {
+        const cx<S> x = buf[swz<S>(u)];
+        buf[swz<S>(u)] = {pe[u], sc<S>::neg(sc<S>::sqsum(x.r, x.i))};
+      }
+      __syncthreads();
+      fft_inverse<S>(buf, 1, M1, a.pm, twm, tid, nthr);
+      cx<S>* z = X + (size_t)h * M1;
+      for (int u = tid; u < M1; u += nthr) z[u] = buf[swz<S>(u)];
+      __syncthreads();
+    }
+
+    // E, F
+    const A total = woff[32];
+    for (int l = tid; l < nl; l += nthr) {
+      const int tau = a.lags[l];
+      if (T - tau <= kDirect) continue;
+      const int kn = tau == 0 ? 0 : N2 - tau;
+      cx<S> yk, yn;
+      if (R0 == 8) {
+        yk = half_first_inverse_at<S, 4>(X, tau, M1, tw);
+        yn = half_first_inverse_at<S, 4>(X, kn, M1, tw);
+      } else if (R0 == 4) {
+        yk = half_first_inverse_at<S, 2>(X, tau, M1, tw);
+        yn = half_first_inverse_at<S, 2>(X, kn, M1, tw);
+      } else {
+        yk = X[tau];
+        yn = X[kn];
+      }
+      const S xe = sc<S>::add(yk.r, yn.r);
+      const cx<S> xo = {sc<S>::neg(sc<S>::add(yk.i, yn.i)), sc<S>::sub(yn.r, yk.r)};
+      const cx<S> w = tw[tau];
+      const S y = sc<S>::add(xe, sc<S>::sub(sc<S>::mul(w.r, xo.r), sc<S>::mul(w.i, xo.i)));
+      const A c2 = sc<A>::mul(cvt<S, A>::to_acc(y), invN);
+      // prefix sums: pfx(x) = sum_{s < x} |G(s)|^2
+      const int xa = T - tau, xb = tau;
+      const A pa = sc<A>::add(woff[(xa - 1) / seg], P[xa - 1]);
+      const A pb = xb == 0 ? sc<A>::zero() : sc<A>::add(woff[(xb - 1) / seg], P[xb - 1]);
+      A num = sc<A>::add(pa, sc<A>::sub(total, pb));
+      num = sc<A>::sub(num, c2);
+      a.out[(size_t)l * a.Q + q] = sc<A>::to_double(num) * a.rcp[l];
+    }
+    for (int l = nl - 1 - warp; l >= 0; l -= nw) {
+      const int tau = a.lags[l];
+      const int m = T - tau;
+      if (m > kDirect) break;
+      A acc = sc<A>::zero();
+      for (int t = lane; t < m; t += 32) {
+        const cx<S> g1 = tail[t + tau - tail0], g0 = head[t];
+        const A dr = sc<A>::sub(cvt<S, A>::to_acc(g1.r), cvt<S, A>::to_acc(g0.r));
+        const A di = sc<A>::sub(cvt<S, A>::to_acc(g1.i), cvt<S, A>::to_acc(g0.i));
+        acc = sc<A>::add(acc, sc<A>::sqsum(dr, di));
+      }
+      acc = warp_sum(acc);
+      if (lane == 0) a.out[(size_t)l * a.Q + q] = sc<A>::to_double(acc) * a.rcp[l];
+    }
+    if (tid == 0) {
+      a.out[(size_t)nl * a.Q + q] = sc<A>::to_double(ps);
+      a.out[(size_t)(nl + 1) * a.Q + q] = sc<A>::to_double(sc<A>::mul(total, invT));
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stage 3 (diff mode).  STAGED: the series is copied to shared memory; else
+// (series longer than shared memory) it is read from the spectrum in global
+// memory.
+// dynamic smem: (STAGED ? T * cx<S> : 0) + 96 * A
+// ---------------------------------------------------------------------------
+template <class S, class A, bool STAGED>
 __global__ void __launch_bounds__(512) k_tdiff(TemporalArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int T = a.T, nl = a.nlags;
-  cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
-  A* scratch = reinterpret_cast<A*>(smem_raw + (size_t)T * sizeof(cx<S>));
+  cx<S>* stage = reinterpret_cast<cx<S>*>(smem_raw);
+  A* scratch = reinterpret_cast<A*>(smem_raw + (STAGED ? (size_t)T * sizeof(cx<S>) : 0));
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
   const cx<S>* F = reinterpret_cast<const cx<S>*>(a.spec);
@@ -543,8 +784,11 @@ __global__ void __launch_bounds__(512) k_tdiff(TemporalArgs a) {
 
   for (size_t q = blockIdx.x; q < a.Q; q += gridDim.x) {
     const cx<S>* src = F + q * a.Tpad;
-    for (int t = tid; t < T; t += nthr) buf[t] = src[t];
-    __syncthreads();
+    const cx<S>* buf = STAGED ? stage : src;
+    if (STAGED) {
+      for (int t = tid; t < T; t += nthr) stage[t] = src[t];
+      __syncthreads();
+    }
 
     A v[3] = {sc<A>::zero(), sc<A>::zero(), sc<A>::zero()};
     for (int t = tid; t < T; t += nthr) {

@@ -84,7 +84,9 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   cudaError_t ce;
   if (!r.inline_tables) {
     if (!get_tables(nx, kind, tx, err) || !get_tables(ny, kind, ty, err)) return 3;
-    if (r.mode == MODE_FFT && (!get_tables(N, kind, tt, err) || !get_tables(N / 2, kind, tt2, err))) return 3;
+    // second temporal table: the half length, or the sub-transform length of the long-series kernel
+    if (r.mode == MODE_FFT && (!get_tables(N, kind, tt, err) || !get_tables(L.long_R0 ? N / L.long_R0 : N / 2, kind, tt2, err)))
+      return 3;
   } else {
     // copy host-computed tables into the workspace (no device allocation)
     unsigned char* tp = ws + L.tables_off;
@@ -109,7 +111,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
       return true;
     };
     if (!upload(nx, tx) || !upload(ny, ty)) return 3;
-    if (r.mode == MODE_FFT && (!upload(N, tt) || !upload(N / 2, tt2))) return 3;
+    if (r.mode == MODE_FFT && (!upload(N, tt) || !upload(L.long_R0 ? N / L.long_R0 : N / 2, tt2))) return 3;
   }
 
   // window in the FFT scalar type
@@ -135,7 +137,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   }
   // slot tables of the prefix sums each lag needs: pfx[T - lag] (A) and pfx[lag] (B)
   int* d_slots = reinterpret_cast<int*>(ws + L.slot_off);
-  if (r.mode == MODE_FFT) {
+  if (r.mode == MODE_FFT && !L.long_R0) {
     std::vector<int> slots(2 * (size_t)(T + 1), -1);
     for (int l = 0; l < nl; ++l) {
       slots[T - r.lags[l]] = l;
@@ -220,37 +222,60 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   ta.Q = Q; ta.Tpad = L.Tpad; ta.T = T; ta.nt = N; ta.nlags = nl;
   size_t smem_t = (size_t)T * sizeof(cx<S>) + 96 * sizeof(A);
   int threads = temporal_threads(T);
+  const bool long_fft = r.mode == MODE_FFT && L.long_R0 > 0;
   if (r.mode == MODE_FFT) {
-    ta.twt = tt.tw; ta.twt2 = tt2.tw;
-    if (!temporal_plan(N, ta.pt) || !half_plan(ta.pt, ta.pt2)) {
-      err = "no temporal plan for length " + std::to_string(N);
-      return 4;
-    }
-    ta.slotA = d_slots; ta.slotB = d_slots + (T + 1);
-    ta.need = ws + L.need_off;
-    const size_t with_need = temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), true);
-    ta.need_in_smem = with_need <= kSmemLimit ? 1 : 0;
-    smem_t = temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), ta.need_in_smem != 0);
     split_ff(1.0 / (double)N, ta.invnt_h, ta.invnt_l);
     ta.invnt_d = 1.0 / (double)N;
-    threads = temporal_threads(N);
+    ta.twt = tt.tw;
+    if (long_fft) {
+      ta.R0 = L.long_R0;
+      ta.M1 = N / L.long_R0;
+      ta.pm = tt2.plan;
+      ta.twm = tt2.tw;
+      ta.xs = ws + L.xs_off;
+      ta.xs_stride = L.xs_stride;
+      ta.xs_pfx_off = L.xs_pfx_off;
+      smem_t = temporal_long_smem(ta.M1, sizeof(cx<S>), sizeof(A));
+      threads = temporal_threads(ta.M1);
+    } else {
+      ta.twt2 = tt2.tw;
+      if (!temporal_plan(N, ta.pt) || !half_plan(ta.pt, ta.pt2)) {
+        err = "no temporal plan for length " + std::to_string(N);
+        return 4;
+      }
+      ta.slotA = d_slots; ta.slotB = d_slots + (T + 1);
+      ta.need = ws + L.need_off;
+      const size_t with_need = temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), true);
+      ta.need_in_smem = with_need <= kSmemLimit ? 1 : 0;
+      smem_t = temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), ta.need_in_smem != 0);
+      threads = temporal_threads(N);
+    }
+  } else if (!L.diff_staged) {
+    smem_t = 96 * sizeof(A);
   }
   ta.lags = d_lags; ta.rcp = d_rcp; ta.out = r.out;
   split_ff(1.0 / (double)T, ta.invT_h, ta.invT_l); ta.invT_d = 1.0 / (double)T;
   int dev = 0, nsm = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (r.mode == MODE_FFT) {
-    if ((ce = allow_smem(k_tfft<S, A>, smem_t)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tfft<S, A>, threads, smem_t);
-  } else {
-    if ((ce = allow_smem(k_tdiff<S, A>, smem_t)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tdiff<S, A>, threads, smem_t);
-  }
+  auto prepare = [&](auto kernel) -> bool {
+    if ((ce = allow_smem(kernel, smem_t)) != cudaSuccess) { err = cudaGetErrorString(ce); return false; }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem_t);
+    return true;
+  };
+  bool prepared;
+  if (long_fft) prepared = prepare(k_tfft_long<S, A>);
+  else if (r.mode == MODE_FFT) prepared = prepare(k_tfft<S, A>);
+  else if (L.diff_staged) prepared = prepare(k_tdiff<S, A, true>);
+  else prepared = prepare(k_tdiff<S, A, false>);
+  if (!prepared) return 3;
   if (occ < 1) { err = "temporal kernel does not fit on an SM (shared memory " + std::to_string(smem_t) + " B)"; return 4; }
-  const unsigned grid = (unsigned)std::min<size_t>(std::min<size_t>(Q, (size_t)occ * nsm), kMaxTemporalCtas);
-  if (r.mode == MODE_FFT) k_tfft<S, A><<<grid, threads, smem_t, st>>>(ta);
-  else k_tdiff<S, A><<<grid, threads, smem_t, st>>>(ta);
+  const unsigned grid = (unsigned)std::min<size_t>(std::min<size_t>(Q, (size_t)occ * nsm),
+                                                   long_fft ? kMaxLongCtas : kMaxTemporalCtas);
+  if (long_fft) k_tfft_long<S, A><<<grid, threads, smem_t, st>>>(ta);
+  else if (r.mode == MODE_FFT) k_tfft<S, A><<<grid, threads, smem_t, st>>>(ta);
+  else if (L.diff_staged) k_tdiff<S, A, true><<<grid, threads, smem_t, st>>>(ta);
+  else k_tdiff<S, A, false><<<grid, threads, smem_t, st>>>(ta);
   if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
   if (evs) cudaEventRecord(evs->ev[2], st);
   count_launches(launches + 1);

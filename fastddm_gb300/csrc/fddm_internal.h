@@ -57,6 +57,13 @@ struct TemporalArgs {
   double invT_d;
   float invnt_h, invnt_l;
   double invnt_d;
+  // long series (k_tfft_long): N = R0 * M1, sub-transforms of length M1
+  int R0, M1;
+  FftPlan pm;             // plan of the length-M1 sub-transforms
+  const void* twm;        // twiddles of length M1
+  void* xs;               // per-CTA global scratch: X (N values), then the prefix sums (T accumulators)
+  size_t xs_stride;       // bytes per CTA
+  size_t xs_pfx_off;      // offset of the prefix sums inside one CTA's scratch
 };
 
 enum Precision { PREC_FF = 0, PREC_F64 = 1, PREC_F32 = 2 };
@@ -101,13 +108,19 @@ struct WorkLayout {
   size_t win_off, win_bytes;
   size_t lags_off, rcp_off, slot_off, need_off;
   size_t tables_off, tables_bytes;  // inline FFT tables (DdmRequest::inline_tables)
+  size_t xs_off, xs_stride, xs_pfx_off;  // long-series temporal scratch (per CTA)
   size_t total;
   int Tpad, Hpad, chunk, pairs_per_block, cols_per_block, frames_per_block;
   int nt_fft;  // temporal transform length actually used (fft mode)
+  int long_R0;  // fft mode: >0 selects the long-series kernel with this first radix
+  int diff_staged;  // diff mode: 1 when the series is staged in shared memory
 };
 
 // Upper bound on the temporal kernel's grid (sizes its per-CTA scratch).
 constexpr int kMaxTemporalCtas = 1024;
+// Upper bound on the long-series temporal kernel's grid (one CTA per SM on
+// current parts; sizes its per-CTA transform scratch).
+constexpr int kMaxLongCtas = 304;
 
 // Cheapest even length >= 2T - 1 for the temporal transform (fft mode).
 int choose_temporal_length(int64_t T);
@@ -116,6 +129,8 @@ int choose_temporal_length(int64_t T);
 // scalar complex) and ea (accumulator); `need_in_smem` selects the layout.
 size_t temporal_fft_smem(int T, int N, int nlags, size_t es, size_t ea, bool need_in_smem);
 constexpr size_t kSmemLimit = 232448;  // 227 KB opt-in per CTA
+// Shared memory of the long-series fft-mode kernel (sub-transforms of length M1).
+size_t temporal_long_smem(int M1, size_t es, size_t ea);
 
 // Thread-local error message reported by fddm_b200_last_error().
 void set_last_error(const std::string& msg);

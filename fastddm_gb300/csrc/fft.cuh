@@ -224,6 +224,24 @@ __device__ __forceinline__ void fft_pass_dispatch(cx<S>* buf, int nfft, int ld, 
   }
 }
 
+// Forward DFT of radix R whose upper half of inputs is zero (even R); odd
+// radices fall back to the full DFT.
+template <class S, int R> __device__ __forceinline__ void dft_halfzero(cx<S>* v) {
+  if constexpr (R == 8) {
+    dft8_halfzero<S, false>(v);
+  } else if constexpr (R == 4) {  // x2 = x3 = 0
+    const cx<S> x0 = v[0], x1 = v[1], x1m = cmul_mi<S, false>(x1);
+    v[0] = badd(x0, x1);
+    v[2] = bsub(x0, x1);
+    v[1] = badd(x0, x1m);
+    v[3] = bsub(x0, x1m);
+  } else if constexpr (R == 2) {  // x1 = 0
+    v[1] = v[0];
+  } else {
+    dft<S, R, false>(v);
+  }
+}
+
 // First forward pass of a single transform whose input is zero at indices >=
 // `limit` (limit <= n/2): those slots are neither loaded nor need to be
 // written beforehand.  With an even radix the upper half of every butterfly is
@@ -239,19 +257,7 @@ __device__ __forceinline__ void fft_first_pass_padded(cx<S>* __restrict__ buf, c
       const int idx = j + r * stride;
       v[r] = (r < R / 2 || R % 2) && idx < limit ? buf[swz<S>(idx)] : czero<S>();
     }
-    if constexpr (R == 8) {
-      dft8_halfzero<S, false>(v);
-    } else if constexpr (R == 4) {  // x2 = x3 = 0
-      const cx<S> x0 = v[0], x1 = v[1], x1m = cmul_mi<S, false>(x1);
-      v[0] = badd(x0, x1);
-      v[2] = bsub(x0, x1);
-      v[1] = badd(x0, x1m);
-      v[3] = bsub(x0, x1m);
-    } else if constexpr (R == 2) {  // x1 = 0
-      v[1] = v[0];
-    } else {
-      dft<S, R, false>(v);
-    }
+    dft_halfzero<S, R>(v);
     if (j != 0) {
 #pragma unroll
       for (int m = 1; m < R; ++m) v[m] = twmul<S>::mul(v[m], tw[j * m]);

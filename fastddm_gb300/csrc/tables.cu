@@ -5,6 +5,7 @@
 #include <cmath>
 #include <algorithm>
 #include <cstring>
+#include <cstdlib>
 #include "fddm_internal.h"
 
 namespace fddm {
@@ -251,6 +252,37 @@ size_t temporal_fft_smem(int T, int N, int nlags, size_t es, size_t ea, bool nee
   return b;
 }
 
+size_t temporal_long_smem(int M1, size_t es, size_t ea) {
+  const size_t g = 128 / es;
+  return round_to(round_to(M1, g) * es + (size_t)M1 * (es / 2), 16) + 64 * es + 160 * ea;
+}
+
+// Long-series kernel: the cheapest even N >= 2T - 1 and first radix R0 whose
+// length-N/R0 sub-transforms fit in shared memory (forward sub-transforms of
+// all N points, inverse ones of N/2).
+static bool choose_long_temporal(int64_t T, size_t es, size_t ea, int force_r0, int& N, int& R0) {
+  const int64_t lo = std::max<int64_t>(2, 2 * T - 1);
+  int64_t hi = 1;
+  while (hi < lo) hi <<= 1;
+  double best = 1e300;
+  N = R0 = 0;
+  for (int64_t n = lo + (lo & 1); n <= hi; n += 2) {
+    for (int r0 : {8, 4, 2}) {
+      if ((force_r0 && r0 != force_r0) || n % r0 || temporal_long_smem((int)(n / r0), es, ea) > kSmemLimit) continue;
+      FftPlan rest;
+      if (!make_plan((int)(n / r0), rest)) continue;
+      double c = padded_cost(r0) * (double)n;
+      for (int s = 0; s < rest.npass; ++s) c += pass_cost(rest.radix[s]) * 1.5 * (double)n;
+      if (c < best) {
+        best = c;
+        N = (int)n;
+        R0 = r0;
+      }
+    }
+  }
+  return N > 0;
+}
+
 size_t spec_elem_bytes(int precision) { return precision == PREC_F32 ? 8 : 16; }
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -259,7 +291,6 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
   if (r.T < 1 || r.H < 1 || r.W < 1) { err = "empty image sequence"; return false; }
   if (r.nx < r.W || r.ny < r.H) { err = "nx, ny must be at least the image width and height"; return false; }
   if (r.T > (1 << 30) || r.nx > (1 << 20) || r.ny > (1 << 20)) { err = "problem too large"; return false; }
-  if (r.mode == MODE_FFT && r.T >= 32767) { err = "fft mode supports at most 32766 frames"; return false; }
   FftPlan p;
   if (!make_plan((int)r.nx, p)) { err = "nx=" + std::to_string(r.nx) + " has a prime factor other than 2, 3, 5, 7, 11, 13"; return false; }
   if (!make_plan((int)r.ny, p)) { err = "ny=" + std::to_string(r.ny) + " has a prime factor other than 2, 3, 5, 7, 11, 13"; return false; }
@@ -301,13 +332,32 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
   chunk = std::max(L.frames_per_block, chunk / L.frames_per_block * L.frames_per_block);
   chunk = (int)std::min<int64_t>(chunk, (r.T + L.frames_per_block - 1) / L.frames_per_block * L.frames_per_block);
   L.chunk = chunk;
-  // temporal kernel shared memory
+  // temporal kernel: the whole transform in shared memory when it fits, else
+  // (fft mode) the long-series kernel with sub-transforms of N / R0, or (diff
+  // mode) the series read from global memory
   const size_t ea = 8;
-  const size_t smem_t = r.mode == MODE_FFT ? temporal_fft_smem((int)r.T, L.nt_fft, (int)r.lags.size(), es, ea, false)
-                                           : (size_t)r.T * es + 96 * ea;
-  if (smem_t > kSmemLimit) {
-    err = "sequence too long for the single-CTA temporal kernel (needs " + std::to_string(smem_t) + " B of shared memory)";
-    return false;
+  L.long_R0 = 0;
+  L.diff_staged = 0;
+  if (r.mode == MODE_FFT) {
+    // the shared-memory kernel indexes its lag slot tables with int16
+    // FDDM_B200_TEMPORAL_SPLIT=2|4|8 forces the long-series kernel with that
+    // first radix (diagnostics and tests of that kernel on short series)
+    const char* fs = std::getenv("FDDM_B200_TEMPORAL_SPLIT");
+    const int force = fs ? std::atoi(fs) : 0;
+    const bool forced = force == 2 || force == 4 || force == 8;
+    if (forced || r.T >= 32767 ||
+        temporal_fft_smem((int)r.T, L.nt_fft, (int)r.lags.size(), es, ea, false) > kSmemLimit) {
+      int n = 0, r0 = 0;
+      if (!choose_long_temporal(r.T, es, ea, forced ? force : 0, n, r0)) {
+        err = "sequence too long for the temporal kernels (" + std::to_string(r.T) +
+              " frames: no transform length splits into sub-transforms that fit in shared memory)";
+        return false;
+      }
+      L.nt_fft = n;
+      L.long_R0 = r0;
+    }
+  } else {
+    L.diff_staged = (size_t)r.T * es + 96 * ea <= kSmemLimit ? 1 : 0;
   }
   size_t off = 0;
   L.spec_off = off; L.spec_bytes = Q * (size_t)L.Tpad * es; off = align_up(off + L.spec_bytes, 256);
@@ -317,13 +367,22 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
   L.rcp_off = off; off = align_up(off + r.lags.size() * sizeof(double) + 8, 256);
   L.slot_off = off; off = align_up(off + 2 * (size_t)(r.T + 1) * sizeof(int), 256);
   L.need_off = off;
-  if (r.mode == MODE_FFT) off = align_up(off + (size_t)kMaxTemporalCtas * (2 * r.lags.size() + 2) * ea, 256);
+  if (r.mode == MODE_FFT && !L.long_R0) off = align_up(off + (size_t)kMaxTemporalCtas * (2 * r.lags.size() + 2) * ea, 256);
+  L.xs_off = off;
+  L.xs_stride = L.xs_pfx_off = 0;
+  if (L.long_R0) {
+    L.xs_pfx_off = align_up((size_t)L.nt_fft * es, 256);
+    L.xs_stride = L.xs_pfx_off + align_up((size_t)r.T * ea, 256);
+    off += (size_t)kMaxLongCtas * L.xs_stride;
+  }
   L.tables_off = off;
   L.tables_bytes = 0;
   if (r.inline_tables) {
     const int kind = r.precision == PREC_FF ? 0 : r.precision == PREC_F64 ? 1 : 2;
     L.tables_bytes = inline_table_bytes((int)r.nx, kind) + inline_table_bytes((int)r.ny, kind);
-    if (r.mode == MODE_FFT) L.tables_bytes += inline_table_bytes(L.nt_fft, kind) + inline_table_bytes(L.nt_fft / 2, kind);
+    if (r.mode == MODE_FFT)
+      L.tables_bytes += inline_table_bytes(L.nt_fft, kind) +
+                        inline_table_bytes(L.long_R0 ? L.nt_fft / L.long_R0 : L.nt_fft / 2, kind);
     off += L.tables_bytes;
   }
   L.total = off;
@@ -342,7 +401,7 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
     L.chunk = c;
     L.rbuf_bytes = (size_t)c * per_frame;
     L.win_off -= shrink; L.lags_off -= shrink; L.rcp_off -= shrink; L.slot_off -= shrink;
-    L.need_off -= shrink; L.tables_off -= shrink;
+    L.need_off -= shrink; L.xs_off -= shrink; L.tables_off -= shrink;
     L.total -= shrink;
   }
   return true;

@@ -130,6 +130,49 @@ def test_shapes_and_radices(fddm, shape, mode):
         _check(r._data, imgs, lags, mode, "ff", window, label=f"{shape} window={window is not None}")
 
 
+@pytest.mark.parametrize("T", [3, 10, 500, 1000, 2000, 6000])
+def test_long_sequences_and_first_radix(fddm, T):
+    """Temporal transforms whose plans start with radix 2, 4 and 8 (N = 6, 20,
+    1024, 2048, 4096, 12288), up to 6000 frames on one CTA per mode."""
+    imgs = _poisson_stack((T, 4, 6), "uint16", seed=T)
+    lags = np.unique(np.concatenate([np.geomspace(1, T - 1, 40).astype(int), [T - 40, T - 33, T - 32, T - 1]]))
+    lags = lags[(lags >= 1) & (lags < T)]
+    r = fddm.ddm(imgs, lags, mode="fft", precision="ff")
+    _check(r._data, imgs, lags, "fft", "ff", label=f"T={T}")
+
+
+def _long_lags(T, n=30):
+    lags = np.unique(np.concatenate([np.geomspace(1, T - 1, n).astype(int), [T - 40, T - 33, T - 32, T - 1]]))
+    return lags[(lags >= 1) & (lags < T)]
+
+
+@pytest.mark.parametrize("split", [2, 4, 8])
+@pytest.mark.parametrize("T", [3, 40, 333, 1000])
+def test_split_temporal_kernel(fddm, monkeypatch, T, split):
+    """The long-series fft kernel (first pass in global memory, sub-transforms
+    of N/split in shared memory), forced on short series for every first radix."""
+    monkeypatch.setenv("FDDM_B200_TEMPORAL_SPLIT", str(split))
+    imgs = _poisson_stack((T, 5, 6), "uint16", seed=T + split)
+    lags = _long_lags(T)
+    w = fddm.window.blackman_harris((5, 6))
+    for precision in ("ff", "f64"):
+        r = fddm.ddm(imgs, lags, mode="fft", window=w, precision=precision)
+        _check(r._data, imgs, lags, "fft", precision, w, label=f"split {split} T={T}")
+
+
+@pytest.mark.parametrize("T,mode,precision", [
+    (7000, "fft", "ff"),     # just past the single-CTA transform: split kernel
+    (20000, "fft", "ff"),
+    (20000, "fft", "f32"),   # f32 switches to the split kernel later (8-byte values)
+    (20000, "diff", "ff"),   # series read from global memory
+])
+def test_long_sequences(fddm, T, mode, precision):
+    imgs = _poisson_stack((T, 4, 6), "uint8", seed=T, level=40.0)
+    lags = _long_lags(T, 20)
+    r = fddm.ddm(imgs, lags, mode=mode, precision=precision)
+    _check(r._data, imgs, lags, mode, precision, label=f"T={T}")
+
+
 def test_config1_all_lags_fft_vs_oracle_and_diff(fddm):
     """64 frames of 128 x 128 uint16 Brownian spots, lags 1..63, no window."""
     from fastddm_gb300.synthetic import CONFIG1, make_stack
