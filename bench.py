@@ -36,6 +36,7 @@ CONFIGS = {
     "small": "CONFIG1",        # 64 x 128^2 uint16, all lags
     "large_tall": "CONFIG3_TALL",  # profiling: the large workload's temporal kernel on 64^2 frames
     "large_wide": "CONFIG3_WIDE",  # profiling: the large workload's spatial kernels on 64 frames
+    "long": "CONFIG_LONG",     # 20000 x 256^2 uint8, 200 log lags (split temporal transform)
     "batch": None,             # 96 uneven stacks in one batch call (run_batch)
     "serve": None,             # Poisson request stream through the serving loop (run_serve)
 }
@@ -44,7 +45,7 @@ CONFIGS = {
 def lags_for(name: str, T: int) -> np.ndarray:
     from fastddm_gb300 import lags as lg
 
-    if name in ("large", "large_tall"):
+    if name in ("large", "large_tall", "long"):
         return np.unique(lg.logspace_int(T - 1, num=200, endpoint=True))
     return np.arange(1, T)
 
@@ -331,10 +332,11 @@ def run_ours(args):
             traffic = json.loads(tfile.read_text()).get(f"{args.config}:{args.mode}:{args.precision}")
         except ValueError:
             traffic = None
-    dominant = "k_tfft" if tp_ms >= sp_ms else "k_rows+k_cols"
-    if dominant == "k_tfft":
+    tkernel = "k_tdiff" if args.mode == "diff" else ("k_tfft_long" if args.config == "long" else "k_tfft")
+    dominant = tkernel if tp_ms >= sp_ms else "k_rows+k_cols"
+    if dominant == tkernel:
         ach = tfft_bytes / (tp_ms / 1000.0) / 1e9
-        tr = traffic.get("k_tfft") if isinstance(traffic, dict) else None
+        tr = traffic.get(tkernel) if isinstance(traffic, dict) else None
     else:
         ach = spatial_bytes / (sp_ms / 1000.0) / 1e9
         tr = traffic.get("spatial") if isinstance(traffic, dict) else None

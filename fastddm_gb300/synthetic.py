@@ -45,6 +45,8 @@ CONFIG3 = Scene(4000, 1024, 1024, 5000, 1.5, 150.0, 1.0, 20.0, 0.05, "uint8", 0)
 # the temporal stage (4000 frames, same lags) and the spatial stage (1024 x 1024 frames)
 CONFIG3_TALL = Scene(4000, 64, 64, 20, 1.5, 150.0, 1.0, 20.0, 0.05, "uint8", 0)
 CONFIG3_WIDE = Scene(64, 1024, 1024, 5000, 1.5, 150.0, 1.0, 20.0, 0.05, "uint8", 0)
+# a long series: 20000 frames of 256 x 256 (the split temporal transform, N = 40960)
+CONFIG_LONG = Scene(20000, 256, 256, 300, 1.5, 150.0, 1.0, 20.0, 0.05, "uint8", 0)
 
 
 def _periodic_profile(pos: np.ndarray, n: int, sigma: float) -> np.ndarray:
