@@ -187,20 +187,27 @@ __device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int 
     }
     const int base = f * ld + blk * M + j;
     cx<S> v[R];
+    if (stride > 1) {
+      // twiddles first (their global loads overlap the shared-memory loads and
+      // the butterfly); w^0 = 1 exactly, so j = 0 needs no branch
+      cx<S> w[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = buf[swz<S>(base + r * stride)];
-    if (!INV) {
-      dft<S, R, false>(v);
-      if (j != 0) {
+      for (int m = 1; m < R; ++m) w[m] = tw[twstep * j * m];
 #pragma unroll
-        for (int m = 1; m < R; ++m) v[m] = twmul<S>::mul(v[m], tw[twstep * j * m]);
+      for (int r = 0; r < R; ++r) v[r] = buf[swz<S>(base + r * stride)];
+      if (!INV) {
+        dft<S, R, false>(v);
+#pragma unroll
+        for (int m = 1; m < R; ++m) v[m] = twmul<S>::mul(v[m], w[m]);
+      } else {
+#pragma unroll
+        for (int m = 1; m < R; ++m) v[m] = twmul<S>::mulc(v[m], w[m]);
+        dft<S, R, true>(v);
       }
-    } else {
-      if (j != 0) {
+    } else {  // last pass: j = 0 only, no twiddles
 #pragma unroll
-        for (int m = 1; m < R; ++m) v[m] = twmul<S>::mulc(v[m], tw[twstep * j * m]);
-      }
-      dft<S, R, true>(v);
+      for (int r = 0; r < R; ++r) v[r] = buf[swz<S>(base + r * stride)];
+      dft<S, R, INV>(v);
     }
 #pragma unroll
     for (int r = 0; r < R; ++r) buf[swz<S>(base + r * stride)] = v[r];
