@@ -557,7 +557,9 @@ template <class S, int R0>
 __device__ __forceinline__ void long_first_pass(const cx<S>* __restrict__ src, cx<S>* __restrict__ X, int T, int M1,
                                                 S msr, S msi, const cx<S>* __restrict__ tw, int tid, int nthr) {
   for (int j = tid; j < M1; j += nthr) {
-    cx<S> v[R0];
+    cx<S> v[R0], w[R0];
+#pragma unroll
+    for (int m = 1; m < R0; ++m) w[m] = tw[j * m];  // w^0 = 1 exactly: no j = 0 branch
 #pragma unroll
     for (int r = 0; r < R0; ++r) {
       const int t = j + r * M1;
@@ -569,10 +571,8 @@ __device__ __forceinline__ void long_first_pass(const cx<S>* __restrict__ src, c
       }
     }
     dft_halfzero<S, R0>(v);
-    if (j != 0) {
 #pragma unroll
-      for (int m = 1; m < R0; ++m) v[m] = twmul<S>::mul(v[m], tw[j * m]);
-    }
+    for (int m = 1; m < R0; ++m) v[m] = twmul<S>::mul(v[m], w[m]);
 #pragma unroll
     for (int m = 0; m < R0; ++m) X[j + m * M1] = v[m];
   }

@@ -258,17 +258,17 @@ __device__ __forceinline__ void fft_first_pass_padded(cx<S>* __restrict__ buf, c
                                                       const cx<S>* __restrict__ tw, int tid, int nthr) {
   const int n = p.n, stride = n / R;
   for (int j = tid; j < stride; j += nthr) {
-    cx<S> v[R];
+    cx<S> v[R], w[R];
+#pragma unroll
+    for (int m = 1; m < R; ++m) w[m] = tw[j * m];  // w^0 = 1 exactly: no j = 0 branch
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int idx = j + r * stride;
       v[r] = (r < R / 2 || R % 2) && idx < limit ? buf[swz<S>(idx)] : czero<S>();
     }
     dft_halfzero<S, R>(v);
-    if (j != 0) {
 #pragma unroll
-      for (int m = 1; m < R; ++m) v[m] = twmul<S>::mul(v[m], tw[j * m]);
-    }
+    for (int m = 1; m < R; ++m) v[m] = twmul<S>::mul(v[m], w[m]);
 #pragma unroll
     for (int r = 0; r < R; ++r) buf[swz<S>(j + r * stride)] = v[r];
   }
