@@ -428,7 +428,6 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
   const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
   const cx<S>* F = reinterpret_cast<const cx<S>*>(a.spec);
   const cx<S>* tw = reinterpret_cast<const cx<S>*>(a.twt);
-  const cx<S>* tw2 = reinterpret_cast<const cx<S>*>(a.twt2);
   const A invT = sc<A>::cst(a.invT_h, a.invT_l, a.invT_d);
   const A invN = sc<A>::cst(a.invnt_h, a.invnt_l, a.invnt_d);
   const int chunk = (T + nthr - 1) / nthr;
@@ -490,7 +489,8 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
     __syncthreads();
     // buf above the half-length transform is free: start loading the next mode
     if (q + gridDim.x < a.Q) prefetch_series<S>(ser, F + (q + gridDim.x) * a.Tpad, T, tid, nthr);
-    fft_inverse<S>(buf, 1, N2, a.pt2, tw2, tid, nthr);
+    // the length-N table serves the half-length passes: w_M^k = tw[k N / M]
+    fft_inverse<S>(buf, 1, N2, a.pt2, tw, tid, nthr, N);
 
     for (int l = tid; l < nl; l += nthr) {
       const int tau = a.lags[l];

@@ -159,14 +159,15 @@ template <class S> __host__ __device__ constexpr int swz_round(int n) {
 
 // ---------------------------------------------------------------------------
 // One in-place pass over `nfft` transforms of length n, stored at logical
-// offset f*ld of the (swizzled) buffer.
+// offset f*ld of the (swizzled) buffer.  `tw` is the twiddle table of length
+// twn (a multiple of n): w_M^k = tw[k * twn / M].
 // ---------------------------------------------------------------------------
 template <class S, int R, bool INV>
 __device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int ld, int n, int M, int lgs,
-                                         int lgb, const cx<S>* __restrict__ tw, int tid, int nthr) {
+                                         int lgb, const cx<S>* __restrict__ tw, int twn, int tid, int nthr) {
   const int stride = M / R;
   const int bpf = n / R;
-  const int twstep = n / M;
+  const int twstep = twn / M;
   const int total = nfft * bpf;
   for (int beta = tid; beta < total; beta += nthr) {
     // power-of-two strides (the common case) index with shifts, others divide
@@ -216,17 +217,17 @@ __device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int 
 
 template <class S, bool INV>
 __device__ __forceinline__ void fft_pass_dispatch(cx<S>* buf, int nfft, int ld, const FftPlan& p, int s,
-                                                  const cx<S>* tw, int tid, int nthr) {
+                                                  const cx<S>* tw, int twn, int tid, int nthr) {
   const int n = p.n, M = p.block[s], lgs = p.lgstride[s], lgb = p.lgbpf[s];
   switch (p.radix[s]) {
-    case 2: fft_pass<S, 2, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
-    case 3: fft_pass<S, 3, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
-    case 4: fft_pass<S, 4, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
-    case 5: fft_pass<S, 5, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
-    case 7: fft_pass<S, 7, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
-    case 8: fft_pass<S, 8, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
-    case 11: fft_pass<S, 11, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
-    case 13: fft_pass<S, 13, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, tid, nthr); break;
+    case 2: fft_pass<S, 2, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
+    case 3: fft_pass<S, 3, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
+    case 4: fft_pass<S, 4, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
+    case 5: fft_pass<S, 5, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
+    case 7: fft_pass<S, 7, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
+    case 8: fft_pass<S, 8, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
+    case 11: fft_pass<S, 11, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
+    case 13: fft_pass<S, 13, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
     default: break;
   }
 }
@@ -289,18 +290,20 @@ __device__ void fft_forward_padded(cx<S>* buf, const FftPlan& p, int limit, cons
   }
   __syncthreads();
   for (int s = 1; s < p.npass; ++s) {
-    fft_pass_dispatch<S, false>(buf, 1, p.n, p, s, tw, tid, nthr);
+    fft_pass_dispatch<S, false>(buf, 1, p.n, p, s, tw, p.n, tid, nthr);
     __syncthreads();
   }
 }
 
 // Forward DIF: natural order in, digit-reversed (perm) order out.
 // Caller synchronises before the call; the function ends with a barrier.
+// twn: length of the twiddle table `tw` (0: p.n).
 template <class S>
 __device__ void fft_forward(cx<S>* buf, int nfft, int ld, const FftPlan& p, const cx<S>* tw, int tid,
-                            int nthr) {
+                            int nthr, int twn = 0) {
+  if (twn == 0) twn = p.n;
   for (int s = 0; s < p.npass; ++s) {
-    fft_pass_dispatch<S, false>(buf, nfft, ld, p, s, tw, tid, nthr);
+    fft_pass_dispatch<S, false>(buf, nfft, ld, p, s, tw, twn, tid, nthr);
     __syncthreads();
   }
 }
@@ -308,9 +311,10 @@ __device__ void fft_forward(cx<S>* buf, int nfft, int ld, const FftPlan& p, cons
 // Inverse (unnormalised, sum_k X_k w^(-jk)): perm order in, natural order out.
 template <class S>
 __device__ void fft_inverse(cx<S>* buf, int nfft, int ld, const FftPlan& p, const cx<S>* tw, int tid,
-                            int nthr) {
+                            int nthr, int twn = 0) {
+  if (twn == 0) twn = p.n;
   for (int s = p.npass - 1; s >= 0; --s) {
-    fft_pass_dispatch<S, true>(buf, nfft, ld, p, s, tw, tid, nthr);
+    fft_pass_dispatch<S, true>(buf, nfft, ld, p, s, tw, twn, tid, nthr);
     __syncthreads();
   }
 }
