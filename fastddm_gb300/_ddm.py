@@ -32,26 +32,9 @@ _backend: Dict[str, Dict[str, Callable]] = {
 }
 
 
-def ddm(
-    img_seq,
-    lags: Iterable[int],
-    *,
-    core: str = "b200",
-    mode: str = "fft",
-    window: Optional[np.ndarray] = None,
-    keep_on_device: bool = True,
-    **kwargs,
-) -> ImageStructureFunction:
-    """Image structure function of ``img_seq`` (shape ``(t, y, x)``) at the given lags.
-
-    Raises RuntimeError for an unknown core or mode, negative lags, lags beyond
-    ``len(img_seq) - 1`` or a window whose shape differs from a frame's; lag 0
-    is removed with a warning.  ``kwargs`` go to the backend (``gpu_id``,
-    ``precision``).  With ``keep_on_device`` the returned object also holds the
-    device copy of its data, used by ``azimuthal_average``.
-    """
-    backend = _backend
-    cores = list(backend.keys())
+def _prepare(img_seq, lags, core: str, mode: str, window):
+    """The front door's checks and derived sizes (``src/python/_ddm.py:128-173``)."""
+    cores = list(_backend.keys())
     modes = ["diff", "fft"]
     if core not in cores:
         raise RuntimeError(f"Unknown core '{core}' selected. Only possible options are {cores}.")
@@ -79,6 +62,30 @@ def ddm(
 
     kx = 2 * np.pi * np.fft.fftfreq(nx)[: (nx // 2 + 1)]
     ky = 2 * np.pi * np.fft.fftshift(np.fft.fftfreq(ny))
+
+    return lags, window, nx, ny, nt, kx, ky
+
+
+def ddm(
+    img_seq,
+    lags: Iterable[int],
+    *,
+    core: str = "b200",
+    mode: str = "fft",
+    window: Optional[np.ndarray] = None,
+    keep_on_device: bool = True,
+    **kwargs,
+) -> ImageStructureFunction:
+    """Image structure function of ``img_seq`` (shape ``(t, y, x)``) at the given lags.
+
+    Raises RuntimeError for an unknown core or mode, negative lags, lags beyond
+    ``len(img_seq) - 1`` or a window whose shape differs from a frame's; lag 0
+    is removed with a warning.  ``kwargs`` go to the backend (``gpu_id``,
+    ``precision``).  With ``keep_on_device`` the returned object also holds the
+    device copy of its data, used by ``azimuthal_average``.
+    """
+    backend = _backend
+    lags, window, nx, ny, nt, kx, ky = _prepare(img_seq, lags, core, mode, window)
 
     if core == "b200" and keep_on_device:
         dev, host = ddm_device(img_seq, lags, nx, ny, nt, window, mode=mode, host_out=True, **kwargs)

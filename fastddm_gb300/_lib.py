@@ -98,6 +98,11 @@ _SIGNATURES = {
         ctypes.c_int,
         [_vp, _u64, _u64, _vp, _vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp],
     ),
+    "fddm_b200_sf_write": (
+        ctypes.c_int,
+        [ctypes.c_char_p, _vp, ctypes.c_int, _u64, _u64, _u64, _u64, _u64, _u64, _vp, _vp, _vp,
+         ctypes.c_double, ctypes.c_double, _vp],
+    ),
 }
 
 _lock = threading.Lock()

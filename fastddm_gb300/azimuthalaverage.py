@@ -69,6 +69,13 @@ class AzimuthalAverage:
     def var_err(self) -> Optional[np.ndarray]:
         return None if self._err is None else self._err[:, -1]
 
+    def save(self, fname: str = "analysis_blob") -> None:
+        """Write the object to ``fname`` (``.aa.ddm`` appended if missing) in the
+        reference's file format (``azimuthalaverage.py:197-212``)."""
+        from ._io import save_aa
+
+        save_aa(self, fname)
+
     @property
     def shape(self) -> Tuple[int, int]:
         return self.data.shape

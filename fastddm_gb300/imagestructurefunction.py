@@ -113,6 +113,14 @@ class ImageStructureFunction:
     def __len__(self) -> int:
         return len(self.data)
 
+    def save(self, fname: str = "analysis_blob", from_device: bool = False) -> None:
+        """Write the object to ``fname`` (``.sf.ddm`` appended if missing) in the
+        reference's file format (``imagestructurefunction.py:279-293``);
+        ``from_device`` streams the device copy of ``_data`` instead of the host array."""
+        from ._io import save_sf
+
+        save_sf(self, fname, from_device)
+
     def set_frame_rate(self, frame_rate: float) -> None:
         self.delta_t = 1 / frame_rate
 

@@ -183,6 +183,29 @@ int fddm_b200_ddm_fft_noalloc(const void* d_img_seq, int dtype, uint64_t length,
                               const uint32_t* lags, uint64_t nlags, uint64_t nx, uint64_t ny, uint64_t nt,
                               const double* d_window, double* d_out, int precision, void* stream);
 
+/* Image structure function file (.sf.ddm): replaces the reference's
+   ImageStructureFunction.save / SFWriter.write_obj
+   (src/python/imagestructurefunction.py:279-293, 409-627; header constants in
+   src/python/_io_common.py:16-17) and writes the same bytes: a 64-byte header
+   ("LL"/"BB", id 73, version 0.3, 'd', the six sizes), _data, kx, ky, tau,
+   pixel_size, delta_t and the seven byte offsets.
+     path          output file (created or truncated; the directory must exist)
+     data          (length + extra, height, width) FP64 in C order: the
+                   structure function rows, then the extra rows (PS, VAR)
+     data_on_device 0: `data` is host memory; 1: device memory, streamed to the
+                   file in 32 MiB chunks through two pinned staging buffers
+                   (allocated on the device's first such call and kept), each
+                   copy overlapping the write of the previous chunk and ordered
+                   after the work queued on `stream`
+     length        number of lags; height = ny; width = nx/2 + 1; extra = 2
+     full_width, full_height  nx, ny of the full plane
+     kx, ky, tau   host arrays of width, height and length values
+   Returns FDDM_ERR_INVALID with the system's message when the file cannot be
+   written.  The call returns when the file is complete. */
+int fddm_b200_sf_write(const char* path, const double* data, int data_on_device, uint64_t length, uint64_t height,
+                       uint64_t width, uint64_t extra, uint64_t full_width, uint64_t full_height, const double* kx,
+                       const double* ky, const double* tau, double pixel_size, double delta_t, void* stream);
+
 /* Diagnostics (no counterpart in the reference, which has no tracing).
    fddm_b200_set_stage_timing(1) makes every following ddm call record CUDA
    events on its stream around the spatial stage (row and column FFT passes)
