@@ -98,6 +98,12 @@ _SIGNATURES = {
         ctypes.c_int,
         [_vp, _u64, _u64, _vp, _vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp],
     ),
+    "fddm_b200_tiff_info": (
+        ctypes.c_int,
+        [ctypes.c_char_p, ctypes.POINTER(_u64), ctypes.POINTER(_u64), ctypes.POINTER(_u64),
+         ctypes.POINTER(ctypes.c_int)],
+    ),
+    "fddm_b200_tiff_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_u64), _u64, _vp, ctypes.c_int]),
     "fddm_b200_sf_write": (
         ctypes.c_int,
         [ctypes.c_char_p, _vp, ctypes.c_int, _u64, _u64, _u64, _u64, _u64, _u64, _vp, _vp, _vp,

@@ -20,6 +20,10 @@
  *   src/cuda/ddm_cuda.h:38     ddm_diff_cuda<T>(...)
  *   src/python/bindings/ddm_bindings.h:25-43   one overload per input dtype
  *   src/python/azimuthalaverage.py:277-478     azimuthal_average_array binning
+ *   src/python/imagestructurefunction.py:409-627  SFWriter (.sf.ddm files)
+ *   src/python/utils.py:23-258                 read_images / tiff2numpy (TIFF ingest)
+ * The file functions (fddm_b200_sf_write, fddm_b200_tiff_*) work on host
+ * memory and files and return when done.
  */
 #ifndef FDDM_B200_H
 #define FDDM_B200_H
@@ -205,6 +209,21 @@ int fddm_b200_ddm_fft_noalloc(const void* d_img_seq, int dtype, uint64_t length,
 int fddm_b200_sf_write(const char* path, const double* data, int data_on_device, uint64_t length, uint64_t height,
                        uint64_t width, uint64_t extra, uint64_t full_width, uint64_t full_height, const double* kx,
                        const double* ky, const double* tau, double pixel_size, double delta_t, void* stream);
+
+/* Image ingest: replaces the reference's TIFF path of read_images /
+   tiff2numpy (src/python/utils.py:23-111, 218-258, through tifffile).
+   Grayscale TIFF files, classic or BigTIFF, either byte order, in strips,
+   uncompressed, LZW (with or without horizontal predictor) or PackBits;
+   8-bit unsigned, 16/32/64-bit signed or unsigned and 32/64-bit float samples.
+   fddm_b200_tiff_info returns the number of pages, their height and width and
+   the FDDM dtype code (all pages must agree).  fddm_b200_tiff_read decodes the
+   listed pages (0-based, any order, repeats allowed) into `dst`, page i of the
+   list at byte offset i * height * width * sample bytes, in host byte order;
+   `nthreads` host threads share the pages (uncompressed strips are read
+   straight into `dst`).  Files the reader cannot decode (tiles, colour, other
+   compressions) return FDDM_ERR_UNSUPPORTED with the reason. */
+int fddm_b200_tiff_info(const char* path, uint64_t* npages, uint64_t* height, uint64_t* width, int* dtype);
+int fddm_b200_tiff_read(const char* path, const uint64_t* pages, uint64_t npages, void* dst, int nthreads);
 
 /* Diagnostics (no counterpart in the reference, which has no tracing).
    fddm_b200_set_stage_timing(1) makes every following ddm call record CUDA

@@ -45,3 +45,20 @@ def test_ddm_save_equals_object_save(built_lib, tmp_path):
     back = fddm.load(path)
     np.testing.assert_array_equal(back._data, r._data)
     np.testing.assert_array_equal(back.tau, r.tau)
+
+
+def test_tiff_ingest_pinned_into_ddm(built_lib, tmp_path):
+    """A TIFF stack decoded into page-locked memory goes through ddm like any array."""
+    import fastddm_gb300 as fddm
+    from fastddm_gb300 import utils
+    from tiffgen import write_tiff
+
+    rng = np.random.default_rng(9)
+    frames = rng.poisson(300.0, size=(48, 40, 56)).astype(np.uint16)
+    p = tmp_path / "stack.tif"
+    write_tiff(p, frames, rows_per_strip=7, compression="lzw", predictor=True)
+    pinned = utils.read_images(str(p), pinned=True)
+    np.testing.assert_array_equal(pinned, frames)
+    a = fddm.ddm(pinned, [1, 3, 20])._data
+    b = fddm.ddm(frames, [1, 3, 20])._data
+    np.testing.assert_array_equal(a, b)
