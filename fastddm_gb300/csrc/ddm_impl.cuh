@@ -141,6 +141,52 @@ template <class A> __device__ __forceinline__ A block_exclusive_scan(A v, A* scr
   return res;
 }
 
+// Exclusive block scan of `v` (returns the prefix; `total` gets the block total)
+// fused with the block sums of u0 and u1 (returned in place), two barriers.
+// `scratch` holds at least 96 values of A.
+template <class A> __device__ __forceinline__ A block_scan_sum2(A v, A& total, A& u0, A& u1, A* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  A inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const A u = shfl_up(inc, o);
+    if (lane >= o) inc = sc<A>::add(inc, u);
+  }
+  u0 = warp_sum(u0);
+  u1 = warp_sum(u1);
+  if (lane == 31) scratch[warp] = inc;
+  if (lane == 0) {
+    scratch[32 + warp] = u0;
+    scratch[64 + warp] = u1;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const A w = lane < nw ? scratch[lane] : sc<A>::zero();
+    A x0 = lane < nw ? scratch[32 + lane] : sc<A>::zero();
+    A x1 = lane < nw ? scratch[64 + lane] : sc<A>::zero();
+    A wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const A u = shfl_up(wi, o);
+      if (lane >= o) wi = sc<A>::add(wi, u);
+    }
+    x0 = warp_sum(x0);
+    x1 = warp_sum(x1);
+    __syncwarp();
+    scratch[lane] = sc<A>::sub(wi, w);  // exclusive warp offsets
+    if (lane == 31) scratch[32] = wi;
+    if (lane == 0) {
+      scratch[33] = x0;
+      scratch[34] = x1;
+    }
+  }
+  __syncthreads();
+  total = scratch[32];
+  u0 = scratch[33];
+  u1 = scratch[34];
+  return sc<A>::add(scratch[warp], sc<A>::sub(inc, v));
+}
+
 // ---------------------------------------------------------------------------
 // Asynchronous global -> shared copies (cp.async), used to prefetch the next
 // mode's time series while the current one is being transformed.
@@ -421,9 +467,14 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
   A* scratch = reinterpret_cast<A*>(tail + kDirect);
   short* slotA = reinterpret_cast<short*>(scratch + 96);
   short* slotB = slotA + (T + 1);
+  // need[] and the per-lag tables in shared memory (a.need_in_smem), else need[] in global scratch
   A* need = a.need_in_smem
                 ? reinterpret_cast<A*>(smem_raw + ((reinterpret_cast<unsigned char*>(slotB + (T + 1)) - smem_raw + 15) & ~15))
                 : reinterpret_cast<A*>(a.need) + (size_t)blockIdx.x * (2 * nl + 2);
+  // per-lag tables: w^tau, 1/(T - tau), tau (addresses recomputed where used)
+#define FDDM_LAG_W reinterpret_cast<cx<S>*>(smem_raw + ((reinterpret_cast<unsigned char*>(need + 2 * nl + 2) - smem_raw + 15) & ~15))
+#define FDDM_LAG_RCP reinterpret_cast<double*>(FDDM_LAG_W + nl)
+#define FDDM_LAG_TAU reinterpret_cast<int*>(FDDM_LAG_RCP + nl)
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
   const cx<S>* F = reinterpret_cast<const cx<S>*>(a.spec);
@@ -433,10 +484,19 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
   const int chunk = (T + nthr - 1) / nthr;
   const int tail0 = T - kDirect;  // first index kept in `tail` (may be negative)
   const int R0 = a.pt.radix[0], M1 = N / R0;
+  const int nref = min(T, 32);  // samples of the reference offset
 
   for (int t = tid; t <= T; t += nthr) {
     slotA[t] = (short)a.slotA[t];
     slotB[t] = (short)a.slotB[t];
+  }
+  if (a.need_in_smem) {
+    for (int l = tid; l < nl; l += nthr) {
+      const int tau = a.lags[l];
+      FDDM_LAG_TAU[l] = tau;
+      FDDM_LAG_RCP[l] = a.rcp[l];
+      FDDM_LAG_W[l] = tw[tau];
+    }
   }
   if (blockIdx.x < a.Q) prefetch_series<S>(ser, F + (size_t)blockIdx.x * a.Tpad, T, tid, nthr);
 
@@ -444,22 +504,27 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
     cp_async_wait_all();
     __syncthreads();
 
-    A v[3] = {sc<A>::zero(), sc<A>::zero(), sc<A>::zero()};
-    for (int t = tid; t < T; t += nthr) {
-      const cx<S> f = ser[swz<S>(t)];
-      const A fr = cvt<S, A>::to_acc(f.r), fi = cvt<S, A>::to_acc(f.i);
-      v[0] = sc<A>::add(v[0], fr);
-      v[1] = sc<A>::add(v[1], fi);
-      v[2] = sc<A>::add(v[2], sc<A>::sqsum(fr, fi));
+    // Reference offset m: the mean of 32 samples spread evenly over the series
+    // (all of them when T < 32), computed identically by every warp, so no
+    // barrier is needed.  D is unchanged by any time-constant offset, and with
+    // G = F - m the Wiener-Khinchin cancellation stays near (VAR + |<F> - m|^2)/D
+    // instead of PS/D, where |<F> - m|^2 is about VAR/32 for samples this far
+    // apart.  PS and VAR follow exactly from the sums of G below.
+    A mr = sc<A>::zero(), mi = sc<A>::zero();
+    if (lane < nref) {
+      const cx<S> f = ser[swz<S>(T >= 32 ? (int)(((long long)lane * T) >> 5) : lane)];
+      mr = cvt<S, A>::to_acc(f.r);
+      mi = cvt<S, A>::to_acc(f.i);
     }
-    block_sum<A, 3>(v, scratch);
-    const A mr = sc<A>::mul(v[0], invT), mi = sc<A>::mul(v[1], invT);
-    const A ps = sc<A>::mul(v[2], invT);
-    const S msr = cvt<S, A>::to_fft(mr), msi = cvt<S, A>::to_fft(mi);
+    mr = shfl_idx(warp_sum(mr), 0);
+    mi = shfl_idx(warp_sum(mi), 0);
+    const A inv_ref = sc<A>::from_double(1.0 / nref);
+    const S msr = cvt<S, A>::to_fft(sc<A>::mul(mr, inv_ref)), msi = cvt<S, A>::to_fft(sc<A>::mul(mi, inv_ref));
 
-    // G = F - <F> into buf[0, T); |G|^2 summed over a contiguous chunk per thread
+    // G = F - m into buf[0, T), over a contiguous chunk per thread: sums of G
+    // and of |G|^2 for the statistics and the prefix sums
     const int t_beg = min(T, tid * chunk), t_end = min(T, t_beg + chunk);
-    A run = sc<A>::zero();
+    A run = sc<A>::zero(), sgr = sc<A>::zero(), sgi = sc<A>::zero();
     for (int t = t_beg; t < t_end; ++t) {
       cx<S> g = ser[swz<S>(t)];
       g.r = sc<S>::sub(g.r, msr);
@@ -467,10 +532,23 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
       buf[swz<S>(t)] = g;
       if (t < kDirect) head[t] = g;
       if (t >= tail0) tail[t - tail0] = g;
-      run = sc<A>::add(run, sc<A>::sqsum(cvt<S, A>::to_acc(g.r), cvt<S, A>::to_acc(g.i)));
+      const A gr = cvt<S, A>::to_acc(g.r), gi = cvt<S, A>::to_acc(g.i);
+      run = sc<A>::add(run, sc<A>::sqsum(gr, gi));
+      sgr = sc<A>::add(sgr, gr);
+      sgi = sc<A>::add(sgi, gi);
     }
-    A total;
-    A pre = block_exclusive_scan<A>(run, scratch, total);
+    A total;  // also left in scratch[32] until the next mode's scan
+    A pre = block_scan_sum2<A>(run, total, sgr, sgi, scratch);
+    if (tid == 0) {
+      // <G> (rounding-size), VAR = <|G|^2> - |<G>|^2, PS = <|G|^2> + 2 Re(conj(m) <G>) + |m|^2
+      const A gmr = sc<A>::mul(sgr, invT), gmi = sc<A>::mul(sgi, invT);
+      const A g2 = sc<A>::mul(total, invT);
+      const A mr = cvt<S, A>::to_acc(msr), mi = cvt<S, A>::to_acc(msi);
+      const A cross = sc<A>::add(sc<A>::mul(mr, gmr), sc<A>::mul(mi, gmi));
+      const A ps = sc<A>::add(sc<A>::add(g2, sc<A>::add(cross, cross)), sc<A>::sqsum(mr, mi));
+      a.out[(size_t)nl * a.Q + q] = sc<A>::to_double(ps);
+      a.out[(size_t)(nl + 1) * a.Q + q] = sc<A>::to_double(sc<A>::sub(g2, sc<A>::sqsum(gmr, gmi)));
+    }
     // prefix sums pfx[t + 1] = sum_{s <= t} |G(s)|^2, stored at the slots the lags need
     for (int t = t_beg; t < t_end; ++t) {
       const cx<S> g = buf[swz<S>(t)];
@@ -492,8 +570,9 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
     // the length-N table serves the half-length passes: w_M^k = tw[k N / M]
     fft_inverse<S>(buf, 1, N2, a.pt2, tw, tid, nthr, N);
 
+    total = scratch[32];
     for (int l = tid; l < nl; l += nthr) {
-      const int tau = a.lags[l];
+      const int tau = a.need_in_smem ? FDDM_LAG_TAU[l] : a.lags[l];
       if (T - tau <= kDirect) continue;
       // Y = conj(Z), Z = DFT_{N/2}(z), in natural order
       const cx<S> yk = buf[swz<S>(tau)];
@@ -502,17 +581,17 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
       // y is twice its real part
       const S xe = sc<S>::add(yk.r, yn.r);
       const cx<S> xo = {sc<S>::neg(sc<S>::add(yk.i, yn.i)), sc<S>::sub(yn.r, yk.r)};
-      const cx<S> w = tw[tau];
+      const cx<S> w = a.need_in_smem ? FDDM_LAG_W[l] : tw[tau];
       const S y = sc<S>::add(xe, sc<S>::sub(sc<S>::mul(w.r, xo.r), sc<S>::mul(w.i, xo.i)));
       // 2 Re C = y / N
       const A c2 = sc<A>::mul(cvt<S, A>::to_acc(y), invN);
       A num = sc<A>::add(need[l], sc<A>::sub(total, need[nl + l]));
       num = sc<A>::sub(num, c2);
-      a.out[(size_t)l * a.Q + q] = sc<A>::to_double(num) * a.rcp[l];
+      a.out[(size_t)l * a.Q + q] = sc<A>::to_double(num) * (a.need_in_smem ? FDDM_LAG_RCP[l] : a.rcp[l]);
     }
     // the last lags: direct differences
     for (int l = nl - 1 - warp; l >= 0; l -= nw) {
-      const int tau = a.lags[l];
+      const int tau = a.need_in_smem ? FDDM_LAG_TAU[l] : a.lags[l];
       const int m = T - tau;
       if (m > kDirect) break;
       A acc = sc<A>::zero();
@@ -523,14 +602,13 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
         acc = sc<A>::add(acc, sc<A>::sqsum(dr, di));
       }
       acc = warp_sum(acc);
-      if (lane == 0) a.out[(size_t)l * a.Q + q] = sc<A>::to_double(acc) * a.rcp[l];
-    }
-    if (tid == 0) {
-      a.out[(size_t)nl * a.Q + q] = sc<A>::to_double(ps);
-      a.out[(size_t)(nl + 1) * a.Q + q] = sc<A>::to_double(sc<A>::mul(total, invT));
+      if (lane == 0) a.out[(size_t)l * a.Q + q] = sc<A>::to_double(acc) * (a.need_in_smem ? FDDM_LAG_RCP[l] : a.rcp[l]);
     }
     __syncthreads();
   }
+#undef FDDM_LAG_W
+#undef FDDM_LAG_RCP
+#undef FDDM_LAG_TAU
 }
 
 // ---------------------------------------------------------------------------

@@ -280,13 +280,13 @@ template <class S>
 __device__ void fft_forward_padded(cx<S>* buf, const FftPlan& p, int limit, const cx<S>* tw, int tid, int nthr) {
   switch (p.radix[0]) {
     case 2: fft_first_pass_padded<S, 2>(buf, p, limit, tw, tid, nthr); break;
-    case 3: fft_first_pass_padded<S, 3>(buf, p, limit, tw, tid, nthr); break;
     case 4: fft_first_pass_padded<S, 4>(buf, p, limit, tw, tid, nthr); break;
-    case 5: fft_first_pass_padded<S, 5>(buf, p, limit, tw, tid, nthr); break;
-    case 7: fft_first_pass_padded<S, 7>(buf, p, limit, tw, tid, nthr); break;
     case 8: fft_first_pass_padded<S, 8>(buf, p, limit, tw, tid, nthr); break;
-    case 11: fft_first_pass_padded<S, 11>(buf, p, limit, tw, tid, nthr); break;
-    default: fft_first_pass_padded<S, 13>(buf, p, limit, tw, tid, nthr); break;
+    default:  // odd first radix (plans for the temporal transform start with 2, 4 or 8): zero-fill, full pass
+      for (int i = limit + tid; i < p.n; i += nthr) buf[swz<S>(i)] = czero<S>();
+      __syncthreads();
+      fft_pass_dispatch<S, false>(buf, 1, p.n, p, 0, tw, p.n, tid, nthr);
+      break;
   }
   __syncthreads();
   for (int s = 1; s < p.npass; ++s) {

@@ -248,7 +248,8 @@ size_t temporal_fft_smem(int T, int N, int nlags, size_t es, size_t ea, bool nee
   // below the next series prefetched from offset round_to(N / 2, g)
   const size_t nbuf = std::max(round_to(N, g), round_to(N / 2, g) + round_to(T, g));
   size_t b = (nbuf + 64) * es + 96 * ea + 2 * (size_t)(T + 1) * sizeof(short);
-  if (need_in_smem) b = round_to(b, 16) + (2 * (size_t)nlags + 2) * ea;
+  // need[] and the per-lag tables (w^tau, 1/(T - tau), tau)
+  if (need_in_smem) b = round_to(round_to(b, 16) + (2 * (size_t)nlags + 2) * ea, 16) + (size_t)nlags * (es + 8 + 4);
   return b;
 }
 
