@@ -257,6 +257,7 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
   // unpack phase (several transforms read at the same permuted slot) hits
   // different banks
   const int ld = nx + swz_group<S>::G;
+  const int lgnx = (nx & (nx - 1)) == 0 ? __ffs(nx) - 1 : -1;
   unsigned char* raw[2] = {smem_raw + (size_t)swz_round<S>(a.pairs_per_block * ld) * sizeof(cx<S>), nullptr};
   raw[1] = raw[0] + a.raw_stage_bytes;
   int b = 0;
@@ -278,7 +279,7 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
     const IN* img = reinterpret_cast<const IN*>(a.img) + t * (size_t)H * W;
     const IN* rimg = reinterpret_cast<const IN*>(raw[b]);
     for (int e = tid; e < np * nx; e += nthr) {
-      const int p = e / nx;
+      const int p = lgnx >= 0 ? e >> lgnx : e / nx;
       const int x = e - p * nx;
       const int y0 = 2 * (pair0 + p);
       S va = sc<S>::zero(), vb = sc<S>::zero();
@@ -334,10 +335,12 @@ __device__ __forceinline__ void cols_issue(const SpatialArgs& a, int item, cx<S>
   const int kc0 = (item % ncg) * CK, tl0 = (item / ncg) * TG;
   const int nk = min(CK, nkx - kc0), ntg = min(TG, a.tc - tl0);
   const cx<S>* R = reinterpret_cast<const cx<S>*>(a.rbuf);
+  const int lgny = (ny & (ny - 1)) == 0 ? __ffs(ny) - 1 : -1;
+  const int lgCK = (CK & (CK - 1)) == 0 ? __ffs(CK) - 1 : -1;
   for (int e = tid; e < NB * ny; e += nthr) {
-    const int c = e / ny;
+    const int c = lgny >= 0 ? e >> lgny : e / ny;
     const int y = e - c * ny;
-    const int tl = c / CK;
+    const int tl = lgCK >= 0 ? c >> lgCK : c / CK;
     const int kc = c - tl * CK;
     cx<S>* dst = &buf[swz<S>(c * ld + y)];
     if (kc < nk && tl < ntg && y < H) cp_async<sizeof(cx<S>)>(dst, &R[((size_t)(tl0 + tl) * nkx + kc0 + kc) * a.Hpad + y]);
