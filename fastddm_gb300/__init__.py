@@ -13,7 +13,9 @@ from ._ddm_b200 import DdmPlan, ddm_device, ddm_diff_b200, ddm_fft_b200
 from ._fftopt import next_fast_len
 from .azimuthalaverage import AzimuthalAverage, azimuthal_average, azimuthal_average_array
 from .imagestructurefunction import ImageStructureFunction
-from ._io import AAReader, SFReader, ddm_save, load
+from ._io import AAReader, ISFReader, SFReader, ddm_save, load
+from .intermediatescatteringfunction import IntermediateScatteringFunction, azavg2isf_estimate
+from .noise_est import estimate_camera_noise
 from . import lags, mask, window
 
 __version__ = "0.1.0"

@@ -1,11 +1,13 @@
-"""Binary files of the image structure function (``.sf.ddm``) and of its
-azimuthal average (``.aa.ddm``), byte-compatible with the reference's writers
-and readers.
+"""Binary files of the image structure function (``.sf.ddm``), its azimuthal
+average (``.aa.ddm``) and the intermediate scattering function (``.isf.ddm``),
+byte-compatible with the reference's writers and readers.
 
 Formats (reference ``src/python/_io_common.py:16-17`` for the version (0, 3)
 and the 64-byte header, ``imagestructurefunction.py:409-627, 629-884`` for
-``.sf.ddm``, ``azimuthalaverage.py:567-753, 755-976`` for ``.aa.ddm``): a
-header with the byte order ("LL"/"BB"), the file identifier (73 or 22), the
+``.sf.ddm``, ``azimuthalaverage.py:567-753, 755-976`` for ``.aa.ddm``,
+``intermediatescatteringfunction.py:213-623`` for ``.isf.ddm``, the ``.aa.ddm``
+layout with another identifier): a header with the byte order ("LL"/"BB"),
+the file identifier (73, 22 or 43), the
 version, the dtype character and the sizes, then the arrays in C order, then
 the byte offsets of every array, written in reverse so that a reader starts
 from the end of the file.
@@ -14,8 +16,8 @@ The ``.sf.ddm`` writer is native (``fddm_b200_sf_write``): from host memory it
 is one sequential write; from device memory it streams the structure function
 through pinned staging buffers, overlapping each device-to-host copy with the
 write of the previous chunk (``ddm_save`` computes and writes a stack without
-ever holding the result in host memory).  ``.aa.ddm`` files are small and are
-written here with ``struct``.
+ever holding the result in host memory).  ``.aa.ddm`` and ``.isf.ddm`` files
+are small and are written here with ``struct``.
 """
 
 from __future__ import annotations
@@ -36,6 +38,7 @@ VERSION = (0, 3)
 HEAD_BYTE_LEN = 64
 SF_ID = 73
 AA_ID = 22
+ISF_ID = 43
 
 try:
     import torch
@@ -242,7 +245,17 @@ class SFReader:
 # ---------------------------------------------------------------------------
 def save_aa(obj: AzimuthalAverage, fname: str = "analysis_blob") -> str:
     """``AzimuthalAverage.save``: write ``obj`` to ``fname`` (``.aa.ddm`` appended if missing)."""
-    path = _with_suffix(fname, ".aa.ddm")
+    return _save_binned(obj, _with_suffix(fname, ".aa.ddm"), AA_ID)
+
+
+def save_isf(obj, fname: str = "analysis_blob") -> str:
+    """``IntermediateScatteringFunction.save``: the ``.aa.ddm`` layout with file identifier 43
+    (``intermediatescatteringfunction.py:213-400``)."""
+    return _save_binned(obj, _with_suffix(fname, ".isf.ddm"), ISF_ID)
+
+
+def _save_binned(obj, path: str, file_id: int) -> str:
+    """Binned (k, tau) data with optional errors, k, tau and bin edges."""
     data = np.ascontiguousarray(obj._data)
     if data.dtype == np.float64:
         fmt = "d"
@@ -255,7 +268,7 @@ def save_aa(obj: AzimuthalAverage, fname: str = "analysis_blob") -> str:
     Nk, dim_t = data.shape
     Nextra = dim_t - Nt
     is_err = obj._err is not None
-    head = ("LL" if sys.byteorder == "little" else "BB").encode() + struct.pack("H", AA_ID)
+    head = ("LL" if sys.byteorder == "little" else "BB").encode() + struct.pack("H", file_id)
     head += struct.pack("BB", *VERSION) + fmt.encode() + struct.pack("QQQ", Nk, Nt, Nextra)
     head += struct.pack("B", 1 if is_err else 0)
     head += bytes(HEAD_BYTE_LEN - len(head))
@@ -278,9 +291,14 @@ def save_aa(obj: AzimuthalAverage, fname: str = "analysis_blob") -> str:
 class AAReader:
     """Reader of ``.aa.ddm`` files (interface of ``azimuthalaverage.py:755-911``)."""
 
+    _id, _kind = AA_ID, "azimuthal average"
+
+    def _make(self, data, err, k, tau, bin_edges):
+        return AzimuthalAverage(data, err, k, tau, bin_edges)
+
     def __init__(self, file: str):
         self._fh = open(file, "rb")
-        self._parser = p = _Parser(self._fh, AA_ID, "azimuthal average")
+        self._parser = p = _Parser(self._fh, self._id, self._kind)
         m = {"Nk": p.read_value(7, "Q")}
         m["Nt"] = p.read_value(0, "Q", 1)
         m["Nextra"] = p.read_value(0, "Q", 1)
@@ -310,8 +328,8 @@ class AAReader:
         m = self._metadata
         shape = (m["Nk"], m["Nt"] + m["Nextra"])
         err = self._parser.read_array(m["err_offset"], shape) if m["is_err"] else None
-        return AzimuthalAverage(self._parser.read_array(m["data_offset"], shape), err, self.get_k(),
-                                self.get_tau(), self.get_bin_edges())
+        return self._make(self._parser.read_array(m["data_offset"], shape), err, self.get_k(), self.get_tau(),
+                          self.get_bin_edges())
 
     def get_k(self) -> np.ndarray:
         return self._parser.read_array(self._metadata["k_offset"], self._metadata["Nk"])
@@ -337,12 +355,26 @@ class AAReader:
         return row if self._metadata["is_err"] else None
 
 
-def load(fname: str) -> Union[ImageStructureFunction, AzimuthalAverage]:
-    """Read a ``.sf.ddm`` or ``.aa.ddm`` file (``src/python/_io.py:14-36``)."""
+class ISFReader(AAReader):
+    """Reader of ``.isf.ddm`` files (interface of ``intermediatescatteringfunction.py:402-559``)."""
+
+    _id, _kind = ISF_ID, "intermediate scattering function"
+
+    def _make(self, data, err, k, tau, bin_edges):
+        from .intermediatescatteringfunction import IntermediateScatteringFunction
+
+        return IntermediateScatteringFunction(data, err, k, tau, bin_edges)
+
+
+def load(fname: str):
+    """Read a ``.sf.ddm``, ``.aa.ddm`` or ``.isf.ddm`` file (``src/python/_io.py:14-36``)."""
     if fname.endswith(".sf.ddm"):
         with SFReader(fname) as f:
             return f.load()
     if fname.endswith(".aa.ddm"):
         with AAReader(fname) as f:
+            return f.load()
+    if fname.endswith(".isf.ddm"):
+        with ISFReader(fname) as f:
             return f.load()
     raise RuntimeError("File extension not recognized.")

@@ -98,6 +98,9 @@ _SIGNATURES = {
         ctypes.c_int,
         [_vp, _u64, _u64, _vp, _vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp],
     ),
+    "fddm_b200_polyfit_noise": (
+        ctypes.c_int, [_vp, _u64, _u64, _vp, _vp, _u64, ctypes.c_double, _vp, _vp, _vp]
+    ),
     "fddm_b200_tiff_info": (
         ctypes.c_int,
         [ctypes.c_char_p, ctypes.POINTER(_u64), ctypes.POINTER(_u64), ctypes.POINTER(_u64),

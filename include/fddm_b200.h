@@ -210,6 +210,23 @@ int fddm_b200_sf_write(const char* path, const double* data, int data_on_device,
                        uint64_t width, uint64_t extra, uint64_t full_width, uint64_t full_height, const double* kx,
                        const double* ky, const double* tau, double pixel_size, double delta_t, void* stream);
 
+/* Camera-noise estimate, "polyfit" mode on the image structure function:
+   replaces the per-pixel numpy.polyfit(tau, D, 2, cov=True) loop of the
+   reference's _noise_polyfit_img_str_func (src/python/noise_est.py:686-756).
+     d_data   device rows of the structure function, row k at d_data + k*ld
+              (ld = ny*(nx/2+1)); rows 0 .. npts-1 are fitted
+     npix     pixels per row (<= ld)
+     x        host abscissae (the first npts lags, tau[:npts])
+     p        host (3, npts) least-squares operator of the quadratic fit
+              (rows: coefficients of x^2, x, 1), cov22 the (2, 2) entry of
+              inv(V^T V) for the Vandermonde matrix V of x
+     d_noise, d_unc  device outputs (npix): the constant term and
+              sqrt(cov22 * residual / (npts - 3)); NaN where row 0 is NaN
+   4 <= npts <= 64 (numpy needs more points than coefficients to scale the
+   covariance). */
+int fddm_b200_polyfit_noise(const double* d_data, uint64_t ld, uint64_t npix, const double* x, const double* p,
+                            uint64_t npts, double cov22, double* d_noise, double* d_unc, void* stream);
+
 /* Image ingest: replaces the reference's TIFF path of read_images /
    tiff2numpy (src/python/utils.py:23-111, 218-258, through tifffile).
    Grayscale TIFF files, classic or BigTIFF, either byte order, in strips,

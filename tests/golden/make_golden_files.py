@@ -45,7 +45,51 @@ def main(root: Path) -> None:
     # container built directly
     avg_noerr = aa.AzimuthalAverage(avg._data[:4].copy(), None, avg.k[:4].copy(), avg.tau.copy(), avg.bin_edges[:4].copy())
     avg_noerr.save(str(HERE / "golden_aa_noerr"))
-    print("wrote", sorted(p.name for p in HERE.glob("golden_*.ddm")))
+    # post-processing on the same objects: the reference's estimate_camera_noise
+    # (src/python/noise_est.py) and azavg2isf_estimate
+    # (src/python/intermediatescatteringfunction.py:733-885)
+    ne = importlib.import_module("fastddm.noise_est")
+    isfm = importlib.import_module("fastddm.intermediatescatteringfunction")
+    post = {}
+    rng = np.random.default_rng(3)
+    mask = rng.random(sf.shape[1:]) > 0.2
+    kr = (0.5, 2.0)
+    aa_cases = {
+        "zero": {}, "min": {}, "high_q": {}, "high_q_range": {"k_min": kr[1], "k_max": kr[0]},
+        "power_spec": {"k_min": kr[0], "k_max": kr[1]}, "var": {"k_min": kr[0], "k_max": kr[1]},
+        "polyfit": {}, "polyfit7": {"num_points": 7},
+    }
+    avg_plain = aa.AzimuthalAverage(avg._data.copy(), None, avg.k.copy(), avg.tau.copy(), avg.bin_edges.copy())
+    for tag, obj in (("aa", avg), ("aa_noerr", avg_plain)):
+        for name, kw in aa_cases.items():
+            mode = name.replace("_range", "").replace("7", "")
+            n, u = ne.estimate_camera_noise(obj, mode=mode, **kw)
+            post[f"{tag}_{name}_noise"], post[f"{tag}_{name}_unc"] = n, u
+    sf_cases = {
+        "zero": {}, "min": {}, "min_mask": {"mask": mask}, "high_q": {}, "high_q_mask": {"k_min": 0.5, "k_max": 2.5, "mask": mask},
+        "power_spec": {"k_min": 0.3, "k_max": 3.0}, "var": {"k_min": 0.3, "k_max": 3.0},
+        "polyfit": {}, "polyfit7": {"num_points": 7},
+    }
+    for name, kw in sf_cases.items():
+        mode = name.replace("_mask", "").replace("7", "")
+        n, u = ne.estimate_camera_noise(sf, mode=mode, **kw)
+        post[f"sf_{name}_noise"], post[f"sf_{name}_unc"] = n, u
+    post["sf_mask"] = mask
+    isf_cases = {
+        "default": {}, "min_ps": {"noise_est": "min", "plateau_est": "power_spec"},
+        "custom": {"noise_est": "custom", "noise": np.linspace(1.0, 2.0, len(avg.k)), "plateau_est": "custom",
+                   "plateau": 2 * avg.var + 3.0},
+    }
+    for name, kw in isf_cases.items():
+        for tag, obj in (("aa", avg), ("aa_noerr", avg_plain)):
+            r = isfm.azavg2isf_estimate(obj, **kw)
+            post[f"isf_{name}_{tag}_data"] = r._data
+            post[f"isf_{name}_{tag}_err"] = r._err
+    post["isf_custom_noise"] = isf_cases["custom"]["noise"]
+    post["isf_custom_plateau"] = isf_cases["custom"]["plateau"]
+    isfm.azavg2isf_estimate(avg).save(str(HERE / "golden_isf"))
+    np.savez_compressed(HERE / "golden_post.npz", **post)
+    print("wrote", sorted(p.name for p in HERE.glob("golden_*")))
 
 
 if __name__ == "__main__":

@@ -90,7 +90,7 @@ def test_file_errors(tmp_path):
     from fastddm_gb300 import AAReader, SFReader, load
 
     with pytest.raises(RuntimeError, match="extension"):
-        load(str(tmp_path / "x.isf.ddm"))
+        load(str(tmp_path / "x.fit.ddm"))
     # an .aa.ddm file is not an image structure function file
     bad = tmp_path / "wrong.sf.ddm"
     bad.write_bytes((GOLDEN / "golden_aa.aa.ddm").read_bytes())
