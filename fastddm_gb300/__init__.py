@@ -16,6 +16,6 @@ from .imagestructurefunction import ImageStructureFunction
 from ._io import AAReader, ISFReader, SFReader, ddm_save, load
 from .intermediatescatteringfunction import IntermediateScatteringFunction, azavg2isf_estimate
 from .noise_est import estimate_camera_noise
-from . import lags, mask, window
+from . import lags, mask, utils, window
 
 __version__ = "0.1.0"
