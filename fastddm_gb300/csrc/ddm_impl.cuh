@@ -619,9 +619,10 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
 // shared memory.  N = R0 M1 (R0 in {2, 4, 8}): the first DIF pass runs from
 // the spectrum into the CTA's global scratch X, the length-M1 sub-transforms
 // run in shared memory.  Per q:
-//   A  mean and PS from coalesced sums
-//   B  G = F - <F>: warp-segmented inclusive prefix sums of |G|^2 into the
-//      global scratch, the first and last kDirect values of G into shared memory
+//   A  reference offset m from 32 spread samples (as in k_tfft)
+//   B  G = F - m: warp-segmented inclusive prefix sums of |G|^2 into the
+//      global scratch, sums of G and |G|^2 (PS, VAR), the first and last
+//      kDirect values of G into shared memory
 //   C  first pass (radix R0, zero-padded input read from the spectrum) into
 //      X[m M1 + j]
 //   D  for h < R0/2: sub-blocks 2h and 2h+1 through the remaining forward
@@ -706,27 +707,27 @@ __global__ void __launch_bounds__(512) k_tfft_long(TemporalArgs a) {
   const A invN = sc<A>::cst(a.invnt_h, a.invnt_l, a.invnt_d);
   const int tail0 = T - kDirect;
   const int seg = ((T + nw - 1) / nw + 31) / 32 * 32;  // warp segment of the prefix sums
+  const int nref = min(T, 32);  // samples of the reference offset
 
   for (size_t q = blockIdx.x; q < a.Q; q += gridDim.x) {
     const cx<S>* src = F + q * a.Tpad;
-    // A
-    A v[3] = {sc<A>::zero(), sc<A>::zero(), sc<A>::zero()};
-    for (int t = tid; t < T; t += nthr) {
-      const cx<S> f = src[t];
-      const A fr = cvt<S, A>::to_acc(f.r), fi = cvt<S, A>::to_acc(f.i);
-      v[0] = sc<A>::add(v[0], fr);
-      v[1] = sc<A>::add(v[1], fi);
-      v[2] = sc<A>::add(v[2], sc<A>::sqsum(fr, fi));
+    // A: reference offset m, the mean of 32 samples spread over the series (as
+    // in k_tfft); PS and VAR follow from the sums of G = F - m in B
+    A mr = sc<A>::zero(), mi = sc<A>::zero();
+    if (lane < nref) {
+      const cx<S> f = src[T >= 32 ? (int)(((long long)lane * T) >> 5) : lane];
+      mr = cvt<S, A>::to_acc(f.r);
+      mi = cvt<S, A>::to_acc(f.i);
     }
-    block_sum<A, 3>(v, scratch);
-    const A mr = sc<A>::mul(v[0], invT), mi = sc<A>::mul(v[1], invT);
-    const A ps = sc<A>::mul(v[2], invT);
-    const S msr = cvt<S, A>::to_fft(mr), msi = cvt<S, A>::to_fft(mi);
+    mr = shfl_idx(warp_sum(mr), 0);
+    mi = shfl_idx(warp_sum(mi), 0);
+    const A inv_ref = sc<A>::from_double(1.0 / nref);
+    const S msr = cvt<S, A>::to_fft(sc<A>::mul(mr, inv_ref)), msi = cvt<S, A>::to_fft(sc<A>::mul(mi, inv_ref));
 
     // B
     {
       const int s0 = warp * seg, s1 = min(T, s0 + seg);
-      A carry = sc<A>::zero();
+      A carry = sc<A>::zero(), sgr = sc<A>::zero(), sgi = sc<A>::zero();
       for (int t0 = s0; t0 < s1; t0 += 32) {
         const int t = t0 + lane;
         A e = sc<A>::zero();
@@ -736,7 +737,10 @@ __global__ void __launch_bounds__(512) k_tfft_long(TemporalArgs a) {
           g.i = sc<S>::sub(g.i, msi);
           if (t < kDirect) head[t] = g;
           if (t >= tail0) tail[t - tail0] = g;
-          e = sc<A>::sqsum(cvt<S, A>::to_acc(g.r), cvt<S, A>::to_acc(g.i));
+          const A gr = cvt<S, A>::to_acc(g.r), gi = cvt<S, A>::to_acc(g.i);
+          e = sc<A>::sqsum(gr, gi);
+          sgr = sc<A>::add(sgr, gr);
+          sgi = sc<A>::add(sgi, gi);
         }
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -747,18 +751,39 @@ __global__ void __launch_bounds__(512) k_tfft_long(TemporalArgs a) {
         if (t < s1) P[t] = inc;
         carry = shfl_idx(inc, 31);
       }
-      if (lane == 0) scratch[warp] = carry;
+      sgr = warp_sum(sgr);
+      sgi = warp_sum(sgi);
+      if (lane == 0) {
+        scratch[warp] = carry;
+        scratch[32 + warp] = sgr;
+        scratch[64 + warp] = sgi;
+      }
       __syncthreads();
       if (warp == 0) {
         const A w = lane < nw ? scratch[lane] : sc<A>::zero();
+        A x0 = lane < nw ? scratch[32 + lane] : sc<A>::zero();
+        A x1 = lane < nw ? scratch[64 + lane] : sc<A>::zero();
         A wi = w;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
           const A u = shfl_up(wi, o);
           if (lane >= o) wi = sc<A>::add(wi, u);
         }
+        x0 = warp_sum(x0);
+        x1 = warp_sum(x1);
+        const A tot = shfl_idx(wi, 31);
         woff[lane] = sc<A>::sub(wi, w);
         if (lane == 31) woff[32] = wi;
+        if (lane == 0) {
+          // <G> (rounding-size), VAR = <|G|^2> - |<G>|^2, PS = <|G|^2> + 2 Re(conj(m) <G>) + |m|^2
+          const A gmr = sc<A>::mul(x0, invT), gmi = sc<A>::mul(x1, invT);
+          const A g2 = sc<A>::mul(tot, invT);
+          const A mr2 = cvt<S, A>::to_acc(msr), mi2 = cvt<S, A>::to_acc(msi);
+          const A cross = sc<A>::add(sc<A>::mul(mr2, gmr), sc<A>::mul(mi2, gmi));
+          const A ps = sc<A>::add(sc<A>::add(g2, sc<A>::add(cross, cross)), sc<A>::sqsum(mr2, mi2));
+          a.out[(size_t)nl * a.Q + q] = sc<A>::to_double(ps);
+          a.out[(size_t)(nl + 1) * a.Q + q] = sc<A>::to_double(sc<A>::sub(g2, sc<A>::sqsum(gmr, gmi)));
+        }
       }
     }
 
@@ -837,10 +862,6 @@ __global__ void __launch_bounds__(512) k_tfft_long(TemporalArgs a) {
       }
       acc = warp_sum(acc);
       if (lane == 0) a.out[(size_t)l * a.Q + q] = sc<A>::to_double(acc) * a.rcp[l];
-    }
-    if (tid == 0) {
-      a.out[(size_t)nl * a.Q + q] = sc<A>::to_double(ps);
-      a.out[(size_t)(nl + 1) * a.Q + q] = sc<A>::to_double(sc<A>::mul(total, invT));
     }
     __syncthreads();
   }

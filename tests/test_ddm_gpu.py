@@ -173,6 +173,25 @@ def test_long_sequences(fddm, T, mode, precision):
     _check(r._data, imgs, lags, mode, precision, label=f"T={T}")
 
 
+def test_long_sequence_window_odd_size_f64(fddm):
+    """Split temporal transform with a window, odd frame sizes (padded FFTs) and the f64 tier."""
+    T = 7001
+    imgs = _poisson_stack((T, 5, 7), "uint16", seed=5)
+    lags = _long_lags(T, 15)
+    w = fddm.window.blackman((5, 7))
+    for precision in ("ff", "f64"):
+        r = fddm.ddm(imgs, lags, mode="fft", window=w, precision=precision)
+        _check(r._data, imgs, lags, "fft", precision, w, label=f"T={T} window")
+
+
+def test_sequence_beyond_the_split_kernel_is_refused(fddm):
+    from fastddm_gb300._lib import FddmError
+
+    imgs = np.zeros((40000, 2, 2), dtype=np.uint8)
+    with pytest.raises(FddmError, match="too long"):
+        fddm.ddm(imgs, [1, 2], mode="fft")
+
+
 def test_config1_all_lags_fft_vs_oracle_and_diff(fddm):
     """64 frames of 128 x 128 uint16 Brownian spots, lags 1..63, no window."""
     from fastddm_gb300.synthetic import CONFIG1, make_stack
