@@ -501,9 +501,9 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
       FDDM_LAG_W[l] = tw[tau];
     }
   }
-  if (blockIdx.x < a.Q) prefetch_series<S>(ser, F + (size_t)blockIdx.x * a.Tpad, T, tid, nthr);
+  if (a.q_begin + blockIdx.x < a.q_end) prefetch_series<S>(ser, F + (a.q_begin + blockIdx.x) * a.Tpad, T, tid, nthr);
 
-  for (size_t q = blockIdx.x; q < a.Q; q += gridDim.x) {
+  for (size_t q = a.q_begin + blockIdx.x; q < a.q_end; q += gridDim.x) {
     cp_async_wait_all();
     __syncthreads();
 
@@ -569,7 +569,7 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
     else pair_power<S, 2>(buf, M1, tid, nthr);
     __syncthreads();
     // buf above the half-length transform is free: start loading the next mode
-    if (q + gridDim.x < a.Q) prefetch_series<S>(ser, F + (q + gridDim.x) * a.Tpad, T, tid, nthr);
+    if (q + gridDim.x < a.q_end) prefetch_series<S>(ser, F + (q + gridDim.x) * a.Tpad, T, tid, nthr);
     // the length-N table serves the half-length passes: w_M^k = tw[k N / M]
     fft_inverse<S>(buf, 1, N2, a.pt2, tw, tid, nthr, N);
 
@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(512) k_tfft_long(TemporalArgs a) {
   const int seg = ((T + nw - 1) / nw + 31) / 32 * 32;  // warp segment of the prefix sums
   const int nref = min(T, 32);  // samples of the reference offset
 
-  for (size_t q = blockIdx.x; q < a.Q; q += gridDim.x) {
+  for (size_t q = a.q_begin + blockIdx.x; q < a.q_end; q += gridDim.x) {
     const cx<S>* src = F + q * a.Tpad;
     // A: reference offset m, the mean of 32 samples spread over the series (as
     // in k_tfft); PS and VAR follow from the sums of G = F - m in B
@@ -884,7 +884,7 @@ __global__ void __launch_bounds__(512) k_tdiff(TemporalArgs a) {
   const cx<S>* F = reinterpret_cast<const cx<S>*>(a.spec);
   const A invT = sc<A>::cst(a.invT_h, a.invT_l, a.invT_d);
 
-  for (size_t q = blockIdx.x; q < a.Q; q += gridDim.x) {
+  for (size_t q = a.q_begin + blockIdx.x; q < a.q_end; q += gridDim.x) {
     const cx<S>* src = F + q * a.Tpad;
     const cx<S>* buf = STAGED ? stage : src;
     if (STAGED) {

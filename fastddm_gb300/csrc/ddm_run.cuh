@@ -270,20 +270,51 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   else prepared = prepare(k_tdiff<S, A, false>);
   if (!prepared) return 3;
   if (occ < 1) { err = "temporal kernel does not fit on an SM (shared memory " + std::to_string(smem_t) + " B)"; return 4; }
-  const unsigned grid = (unsigned)std::min<size_t>(std::min<size_t>(Q, (size_t)occ * nsm),
-                                                   long_fft ? kMaxLongCtas : kMaxTemporalCtas);
-  if (long_fft) k_tfft_long<S, A><<<grid, threads, smem_t, st>>>(ta);
-  else if (r.mode == MODE_FFT) k_tfft<S, A><<<grid, threads, smem_t, st>>>(ta);
-  else if (L.diff_staged) k_tdiff<S, A, true><<<grid, threads, smem_t, st>>>(ta);
-  else k_tdiff<S, A, false><<<grid, threads, smem_t, st>>>(ta);
-  if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+  const size_t max_grid = std::min<size_t>((size_t)occ * nsm, long_fft ? kMaxLongCtas : kMaxTemporalCtas);
+  // With a host result the modes run in chunks: each chunk's output columns
+  // (all lag rows) go to the host with a 2D copy on the copy stream while the
+  // next chunk computes, so only the last chunk's copy is exposed.
+  const int nchunks = (r.host_out && Q >= 16 * max_grid) ? 4 : 1;
+  CopyCtx* cpo = nullptr;
+  if (nchunks > 1 && !(cpo = copy_ctx(err))) return 3;
+  for (int c = 0; c < nchunks; ++c) {
+    ta.q_begin = Q * c / nchunks;
+    ta.q_end = Q * (c + 1) / nchunks;
+    const unsigned grid = (unsigned)std::min<size_t>(ta.q_end - ta.q_begin, max_grid);
+    if (grid == 0) continue;
+    if (long_fft) k_tfft_long<S, A><<<grid, threads, smem_t, st>>>(ta);
+    else if (r.mode == MODE_FFT) k_tfft<S, A><<<grid, threads, smem_t, st>>>(ta);
+    else if (L.diff_staged) k_tdiff<S, A, true><<<grid, threads, smem_t, st>>>(ta);
+    else k_tdiff<S, A, false><<<grid, threads, smem_t, st>>>(ta);
+    if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+    if (cpo) {
+      const size_t pitch = Q * sizeof(double);
+      if ((ce = cudaEventRecord(cpo->ready, st)) != cudaSuccess ||
+          (ce = cudaStreamWaitEvent(cpo->stream, cpo->ready, 0)) != cudaSuccess ||
+          (ce = cudaMemcpy2DAsync(r.host_out + ta.q_begin, pitch, r.out + ta.q_begin, pitch,
+                                  (ta.q_end - ta.q_begin) * sizeof(double), (size_t)nl + 2, cudaMemcpyDeviceToHost,
+                                  cpo->stream)) != cudaSuccess) {
+        err = cudaGetErrorString(ce);
+        return 3;
+      }
+    }
+  }
   if (evs) cudaEventRecord(evs->ev[2], st);
-  count_launches(launches + 1);
+  count_launches(launches + nchunks);
   if (r.host_out) {
-    const size_t bytes = (size_t)(nl + 2) * Q * sizeof(double);
-    if ((ce = cudaMemcpyAsync(r.host_out, r.out, bytes, cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
-      err = cudaGetErrorString(ce);
-      return 3;
+    if (cpo) {
+      // work queued on `stream` after this call sees the copies done
+      if ((ce = cudaEventRecord(cpo->start, cpo->stream)) != cudaSuccess ||
+          (ce = cudaStreamWaitEvent(st, cpo->start, 0)) != cudaSuccess) {
+        err = cudaGetErrorString(ce);
+        return 3;
+      }
+    } else {
+      const size_t bytes = (size_t)(nl + 2) * Q * sizeof(double);
+      if ((ce = cudaMemcpyAsync(r.host_out, r.out, bytes, cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
+        err = cudaGetErrorString(ce);
+        return 3;
+      }
     }
   }
   return 0;

@@ -41,7 +41,8 @@ struct SpatialArgs {
 
 struct TemporalArgs {
   const void* spec;
-  size_t Q;
+  size_t Q;                // modes (the output's row stride)
+  size_t q_begin, q_end;   // modes of this launch
   int Tpad, T, nt, nlags;  // nt: the temporal transform length N chosen by plan_layout
   FftPlan pt, pt2;         // plan for N and the half-length plan derived from it (half_plan)
   const void* twt;         // twiddles of length N

@@ -192,6 +192,16 @@ def test_sequence_beyond_the_split_kernel_is_refused(fddm):
         fddm.ddm(imgs, [1, 2], mode="fft")
 
 
+@pytest.mark.parametrize("mode", ["fft", "diff"])
+def test_chunked_host_result_equals_device_result(fddm, mode):
+    """With a host result the temporal stage runs in chunks of modes whose columns are copied to
+    the host while the next chunk computes; the host array must equal the device array."""
+    imgs = _poisson_stack((24, 96, 128), "uint16", seed=3)  # 6240 modes: chunked
+    r = fddm.ddm(imgs, [1, 2, 5, 11, 23], mode=mode)
+    np.testing.assert_array_equal(r._data, r._device_data.cpu().numpy())
+    _check(r._data, imgs, [1, 2, 5, 11, 23], mode, "ff", label="chunked")
+
+
 def test_config1_all_lags_fft_vs_oracle_and_diff(fddm):
     """64 frames of 128 x 128 uint16 Brownian spots, lags 1..63, no window."""
     from fastddm_gb300.synthetic import CONFIG1, make_stack
