@@ -367,7 +367,8 @@ def run_ours(args):
             del res
         e2e = {"value": T / statistics.mean(times), "unit": "frames/s",
                "h2d_bytes_per_step": int(host.numel() * host.element_size()),
-               "d2h_bytes_per_step": int(nbytes_out), "ms_per_step": 1000 * statistics.mean(times)}
+               "d2h_bytes_per_step": int(nbytes_out), "ms_per_step": 1000 * statistics.mean(times),
+               "step_ms": [round(1000 * t, 2) for t in times]}
 
     cpu = None
     if not args.no_cpu and rank == 0 and ws == 1:

@@ -202,6 +202,19 @@ def test_chunked_host_result_equals_device_result(fddm, mode):
     _check(r._data, imgs, [1, 2, 5, 11, 23], mode, "ff", label="chunked")
 
 
+def test_concurrent_calls(fddm):
+    """Calls from several threads at once give the same results as sequential calls."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    stacks = [_poisson_stack((32, 48, 64), "uint16", seed=s) for s in range(4)]
+    lags = [1, 2, 7, 31]
+    ref = [fddm.ddm(x, lags)._data for x in stacks]
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        got = list(ex.map(lambda x: fddm.ddm(x, lags)._data, stacks * 2))
+    for i, g in enumerate(got):
+        np.testing.assert_array_equal(g, ref[i % 4])
+
+
 def test_config1_all_lags_fft_vs_oracle_and_diff(fddm):
     """64 frames of 128 x 128 uint16 Brownian spots, lags 1..63, no window."""
     from fastddm_gb300.synthetic import CONFIG1, make_stack
