@@ -82,6 +82,10 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   FftTables tx, ty, tt, tt2;
   const int N = L.nt_fft;
   cudaError_t ce;
+  // workspace-only mode: the pass-table area of each uploaded length, in upload order (nx, ny, N, second)
+  unsigned char* pass_area[4] = {nullptr, nullptr, nullptr, nullptr};
+  int pass_n[4] = {0, 0, 0, 0};
+  int nregion = 0;
   if (!r.inline_tables) {
     if (!get_tables(nx, kind, tx, err) || !get_tables(ny, kind, ty, err)) return 3;
     // second temporal table: the half length, or the sub-transform length of the long-series kernel
@@ -107,6 +111,8 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
       t.tw = twp;
       t.perm = pp;
       t.iperm = ip;
+      pass_area[nregion] = tp + up(h->tw.size()) + 2 * up(sizeof(int) * (size_t)n);
+      pass_n[nregion++] = n;
       tp += inline_table_bytes(n, kind);
       return true;
     };
@@ -163,6 +169,17 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   sa.cols_per_block = L.cols_per_block;
   sa.frames_per_block = L.frames_per_block;
   sa.px = tx.plan; sa.py = ty.plan;
+  // per-pass twiddle tables (coalesced twiddle loads); region i of the
+  // workspace-only mode holds the tables of the i-th uploaded length
+  auto attach = [&](FftPlan& p, int region) -> bool {
+    if (!r.inline_tables) return attach_pass_tables(p, kind, err);
+    if (region >= nregion || !pass_area[region]) {
+      err = "no workspace area for the pass twiddle tables";
+      return false;
+    }
+    return upload_pass_tables(p, kind, pass_area[region], pass_tables_bound(pass_n[region], kind), st, err);
+  };
+  if (!attach(sa.px, 0) || !attach(sa.py, 1)) return 3;
   sa.twx = tx.tw; sa.twy = ty.tw; sa.permx = tx.perm; sa.permy = ty.perm;
   sa.rbuf = ws + L.rbuf_off;
   sa.spec = ws + L.spec_off;
@@ -231,6 +248,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
       ta.R0 = L.long_R0;
       ta.M1 = N / L.long_R0;
       ta.pm = tt2.plan;
+      if (!attach(ta.pm, 3)) return 3;
       ta.twm = tt2.tw;
       ta.xs = ws + L.xs_off;
       ta.xs_stride = L.xs_stride;
@@ -243,6 +261,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
         err = "no temporal plan for length " + std::to_string(N);
         return 4;
       }
+      if (!attach(ta.pt, 2) || !attach(ta.pt2, 3)) return 3;
       ta.slotA = d_slots; ta.slotB = d_slots + (T + 1);
       ta.need = ws + L.need_off;
       const size_t with_need = temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), true);

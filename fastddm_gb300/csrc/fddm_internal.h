@@ -18,6 +18,10 @@ struct FftPlan {
   int block[kMaxPass];  // block size M_s at pass s (M_0 = n)
   int lgstride[kMaxPass];  // log2(M_s / R_s) when a power of two, else -1
   int lgbpf[kMaxPass];     // log2(n / R_s) when a power of two, else -1
+  // per-pass twiddle tables (device, null when not attached or stride 1): pass
+  // s reads w_M^(j m) at ptw[s][(m - 1) * stride + j], contiguous in j, so a
+  // warp's twiddle loads are coalesced (attach_pass_tables)
+  const void* ptw[kMaxPass];
 };
 
 struct SpatialArgs {
@@ -164,6 +168,14 @@ bool temporal_plan(int n, FftPlan& p);
 int run_ddm_ff(const DdmRequest& r, cudaStream_t st, std::string& err);
 int run_ddm_f64(const DdmRequest& r, cudaStream_t st, std::string& err);
 int run_ddm_f32(const DdmRequest& r, cudaStream_t st, std::string& err);
+
+// Attach the cached per-device pass twiddle tables of `p` (kind as get_tables).
+bool attach_pass_tables(FftPlan& p, int kind, std::string& err);
+// Workspace-only mode: copy the pass tables of `p` to `dst` (at most `room`
+// bytes, 256-byte aligned parts) on `st` and attach them.
+bool upload_pass_tables(FftPlan& p, int kind, unsigned char* dst, size_t room, cudaStream_t st, std::string& err);
+// Bytes the pass tables of any plan of length n take in a workspace (bound).
+size_t pass_tables_bound(int n, int kind);
 
 // Cached per-device FFT tables (twiddles in the requested scalar format, permutation).
 struct FftTables {

@@ -159,15 +159,16 @@ template <class S> __host__ __device__ constexpr int swz_round(int n) {
 
 // ---------------------------------------------------------------------------
 // One in-place pass over `nfft` transforms of length n, stored at logical
-// offset f*ld of the (swizzled) buffer.  `tw` is the twiddle table of length
-// twn (a multiple of n): w_M^k = tw[k * twn / M].
+// offset f*ld of the (swizzled) buffer.  The twiddles w_M^(j m) come from the
+// pass table `ptw` (FftPlan::ptw, row m - 1, column j), read contiguously by
+// consecutive butterflies; stride-1 passes have none.
 // ---------------------------------------------------------------------------
 template <class S, int R, bool INV>
 __device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int ld, int n, int M, int lgs,
-                                         int lgb, const cx<S>* __restrict__ tw, int twn, int tid, int nthr) {
+                                         int lgb, const cx<S>* __restrict__ tw, int twn,
+                                         const cx<S>* __restrict__ ptw, int tid, int nthr) {
   const int stride = M / R;
   const int bpf = n / R;
-  const int twstep = twn / M;
   const int total = nfft * bpf;
   for (int beta = tid; beta < total; beta += nthr) {
     // power-of-two strides (the common case) index with shifts, others divide
@@ -193,7 +194,7 @@ __device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int 
       // the butterfly); w^0 = 1 exactly, so j = 0 needs no branch
       cx<S> w[R];
 #pragma unroll
-      for (int m = 1; m < R; ++m) w[m] = tw[twstep * j * m];
+      for (int m = 1; m < R; ++m) w[m] = ptw[(m - 1) * stride + j];
 #pragma unroll
       for (int r = 0; r < R; ++r) v[r] = buf[swz<S>(base + r * stride)];
       if (!INV) {
@@ -219,15 +220,16 @@ template <class S, bool INV>
 __device__ __forceinline__ void fft_pass_dispatch(cx<S>* buf, int nfft, int ld, const FftPlan& p, int s,
                                                   const cx<S>* tw, int twn, int tid, int nthr) {
   const int n = p.n, M = p.block[s], lgs = p.lgstride[s], lgb = p.lgbpf[s];
+  const cx<S>* ptw = reinterpret_cast<const cx<S>*>(p.ptw[s]);
   switch (p.radix[s]) {
-    case 2: fft_pass<S, 2, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
-    case 3: fft_pass<S, 3, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
-    case 4: fft_pass<S, 4, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
-    case 5: fft_pass<S, 5, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
-    case 7: fft_pass<S, 7, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
-    case 8: fft_pass<S, 8, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
-    case 11: fft_pass<S, 11, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
-    case 13: fft_pass<S, 13, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, tid, nthr); break;
+    case 2: fft_pass<S, 2, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
+    case 3: fft_pass<S, 3, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
+    case 4: fft_pass<S, 4, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
+    case 5: fft_pass<S, 5, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
+    case 7: fft_pass<S, 7, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
+    case 8: fft_pass<S, 8, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
+    case 11: fft_pass<S, 11, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
+    case 13: fft_pass<S, 13, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
     default: break;
   }
 }
@@ -258,10 +260,11 @@ template <class S, int R>
 __device__ __forceinline__ void fft_first_pass_padded(cx<S>* __restrict__ buf, const FftPlan& p, int limit,
                                                       const cx<S>* __restrict__ tw, int tid, int nthr) {
   const int n = p.n, stride = n / R;
+  const cx<S>* ptw = reinterpret_cast<const cx<S>*>(p.ptw[0]);
   for (int j = tid; j < stride; j += nthr) {
     cx<S> v[R], w[R];
 #pragma unroll
-    for (int m = 1; m < R; ++m) w[m] = tw[j * m];  // w^0 = 1 exactly: no j = 0 branch
+    for (int m = 1; m < R; ++m) w[m] = ptw[(m - 1) * stride + j];  // w^0 = 1: no j = 0 branch
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int idx = j + r * stride;

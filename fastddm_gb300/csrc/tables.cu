@@ -19,6 +19,7 @@ static void finish_plan(FftPlan& p) {
     return l;
   };
   p.lgn = lg(p.n);
+  for (int s = 0; s < kMaxPass; ++s) p.ptw[s] = nullptr;
   int M = p.n;
   for (int s = 0; s < p.npass; ++s) {
     p.block[s] = M;
@@ -132,7 +133,99 @@ bool host_tables(int n, int kind, const HostTables*& out, std::string& err) {
 
 size_t inline_table_bytes(int n, int kind) {
   auto up = [](size_t x) { return (x + 255) / 256 * 256; };
-  return up((size_t)n * (kind == 2 ? 8 : 16)) + 2 * up((size_t)n * sizeof(int));
+  return up((size_t)n * (kind == 2 ? 8 : 16)) + 2 * up((size_t)n * sizeof(int)) + pass_tables_bound(n, kind);
+}
+
+namespace {
+std::mutex g_pass_mu;
+std::map<std::tuple<int, int, int, int>, void*> g_pass_cache;  // (device, M, R, kind) -> device table
+std::mutex g_hpass_mu;
+std::map<std::tuple<int, int, int>, std::vector<unsigned char>> g_hpass_cache;  // (M, R, kind) -> host table
+
+// w_M^(j m), rows m = 1..R-1, columns j = 0..M/R-1, extended precision, in the tier's format
+const std::vector<unsigned char>& host_pass_table(int M, int R, int kind) {
+  std::lock_guard<std::mutex> lk(g_hpass_mu);
+  auto key = std::make_tuple(M, R, kind);
+  auto it = g_hpass_cache.find(key);
+  if (it != g_hpass_cache.end()) return it->second;
+  const int stride = M / R;
+  const size_t esz = kind == 2 ? 8 : 16;
+  std::vector<unsigned char> out(esz * (size_t)(R - 1) * stride, 0);
+  for (int m = 1; m < R; ++m)
+    for (int j = 0; j < stride; ++j) {
+      const long double ang = -2.0L * kPi * (long double)(((long long)j * m) % M) / (long double)M;
+      const long double c = cosl(ang), sn = sinl(ang);
+      unsigned char* dst = &out[esz * ((size_t)(m - 1) * stride + j)];
+      if (kind == 0) {
+        float v[4];
+        v[0] = (float)c; v[1] = (float)(c - (long double)v[0]);
+        v[2] = (float)sn; v[3] = (float)(sn - (long double)v[2]);
+        memcpy(dst, v, sizeof(v));
+      } else if (kind == 1) {
+        double v[2] = {(double)c, (double)sn};
+        memcpy(dst, v, sizeof(v));
+      } else {
+        float v[2] = {(float)c, (float)sn};
+        memcpy(dst, v, sizeof(v));
+      }
+    }
+  return g_hpass_cache.emplace(key, std::move(out)).first->second;
+}
+size_t up256(size_t x) { return (x + 255) / 256 * 256; }
+}  // namespace
+
+size_t pass_tables_bound(int n, int kind) {
+  // a plan's tables hold sum_s (R_s - 1) M_s / R_s < 2 n entries
+  return up256(2 * (size_t)n * (kind == 2 ? 8 : 16)) + (size_t)kMaxPass * 256;
+}
+
+bool attach_pass_tables(FftPlan& p, int kind, std::string& err) {
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return false; }
+  for (int s = 0; s < p.npass; ++s) {
+    const int M = p.block[s], R = p.radix[s];
+    p.ptw[s] = nullptr;
+    if (M / R <= 1) continue;
+    const auto& h = host_pass_table(M, R, kind);
+    std::lock_guard<std::mutex> lk(g_pass_mu);
+    auto key = std::make_tuple(dev, M, R, kind);
+    auto it = g_pass_cache.find(key);
+    if (it == g_pass_cache.end()) {
+      void* d = nullptr;
+      if ((ce = cudaMalloc(&d, h.size())) != cudaSuccess ||
+          (ce = cudaMemcpy(d, h.data(), h.size(), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        if (d) cudaFree(d);
+        err = std::string("FFT pass table upload failed: ") + cudaGetErrorString(ce);
+        return false;
+      }
+      it = g_pass_cache.emplace(key, d).first;
+    }
+    p.ptw[s] = it->second;
+  }
+  return true;
+}
+
+bool upload_pass_tables(FftPlan& p, int kind, unsigned char* dst, size_t room, cudaStream_t st, std::string& err) {
+  size_t used = 0;
+  for (int s = 0; s < p.npass; ++s) {
+    const int M = p.block[s], R = p.radix[s];
+    p.ptw[s] = nullptr;
+    if (M / R <= 1) continue;
+    const auto& h = host_pass_table(M, R, kind);  // cached: stays valid for the asynchronous copy
+    if (used + up256(h.size()) > room) {
+      err = "workspace table area too small for the pass twiddle tables";
+      return false;
+    }
+    const cudaError_t ce = cudaMemcpyAsync(dst + used, h.data(), h.size(), cudaMemcpyHostToDevice, st);
+    if (ce != cudaSuccess) {
+      err = cudaGetErrorString(ce);
+      return false;
+    }
+    p.ptw[s] = dst + used;
+    used += up256(h.size());
+  }
+  return true;
 }
 
 bool get_tables(int n, int kind, FftTables& out, std::string& err) {
