@@ -258,6 +258,7 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
   // different banks
   const int ld = nx + swz_group<S>::G;
   const int lgnx = (nx & (nx - 1)) == 0 ? __ffs(nx) - 1 : -1;
+  const bool u8_fast = sizeof(IN) == 1 && async_raw && !win && W == nx && lgnx >= 2;
   unsigned char* raw[2] = {smem_raw + (size_t)swz_round<S>(a.pairs_per_block * ld) * sizeof(cx<S>), nullptr};
   raw[1] = raw[0] + a.raw_stage_bytes;
   int b = 0;
@@ -278,6 +279,25 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
     }
     const IN* img = reinterpret_cast<const IN*>(a.img) + t * (size_t)H * W;
     const IN* rimg = reinterpret_cast<const IN*>(raw[b]);
+    if (u8_fast) {
+      // 8-bit staged rows without padding or window: four pixels of each row
+      // per 32-bit shared load, converted exactly as 2^23 + b - 2^23
+      const int nq = np * (nx >> 2), lgq = lgnx - 2;
+      const unsigned char* rb = reinterpret_cast<const unsigned char*>(raw[b]);
+      for (int e = tid; e < nq; e += nthr) {
+        const int p = e >> lgq;
+        const int x0 = (e - (p << lgq)) << 2;
+        const int y0 = 2 * (pair0 + p);
+        const uint32_t wa = *reinterpret_cast<const uint32_t*>(rb + (size_t)(2 * p) * W + x0);
+        const uint32_t wb = y0 + 1 < H ? *reinterpret_cast<const uint32_t*>(rb + (size_t)(2 * p + 1) * W + x0) : 0u;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float fa = __fsub_rn(__int_as_float(0x4B000000 | ((wa >> (8 * k)) & 0xFFu)), 8388608.0f);
+          const float fb = __fsub_rn(__int_as_float(0x4B000000 | ((wb >> (8 * k)) & 0xFFu)), 8388608.0f);
+          buf[swz<S>(p * ld + x0 + k)] = {sc<S>::from_float(fa), sc<S>::from_float(fb)};
+        }
+      }
+    } else
     for (int e = tid; e < np * nx; e += nthr) {
       const int p = lgnx >= 0 ? e >> lgnx : e / nx;
       const int x = e - p * nx;

@@ -111,6 +111,17 @@ def test_dtypes(fddm, precision, mode, dtype):
     _check(r._data, imgs, lags, mode, precision, label=dtype)
 
 
+@pytest.mark.parametrize("shape", [(12, 33, 64), (10, 32, 32), (6, 7, 16)])
+def test_uint8_staged_rows(fddm, shape):
+    """8-bit frames with power-of-two widths, staged rows and no window take the row pass's
+    four-pixels-per-load path (odd heights leave the last pair half empty)."""
+    imgs = _poisson_stack(shape, "uint8", seed=sum(shape), level=30.0)
+    lags = sorted({1, 2, shape[0] // 2, shape[0] - 1})
+    for mode in ("fft", "diff"):
+        r = fddm.ddm(imgs, lags, mode=mode)
+        _check(r._data, imgs, lags, mode, "ff", label=f"u8 {shape}")
+
+
 @pytest.mark.parametrize("shape", [
     (7, 13, 11),     # radices 13 and 11, nt = 14 (2 x 7)
     (9, 25, 49),     # 5 x 5 and 7 x 7
