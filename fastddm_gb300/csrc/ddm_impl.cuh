@@ -318,23 +318,18 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
     __syncthreads();
     fft_forward<S>(buf, np, ld, a.px, reinterpret_cast<const cx<S>*>(a.twx), tid, nthr);
 
-    // unpack Z = A + iB into the spectra of the two real rows; write R[tl][k][y]
-    const int ny2 = 2 * np;
-    const int lg2 = (ny2 & (ny2 - 1)) == 0 ? __ffs(ny2) - 1 : -1;
+    // unpack Z = A + iB into the spectra of the two real rows of each pair,
+    // one thread per (k, pair): R[tl][k][2p] and R[tl][k][2p + 1]
+    const int lgp = (np & (np - 1)) == 0 ? __ffs(np) - 1 : -1;
     cx<S>* R = reinterpret_cast<cx<S>*>(a.rbuf) + (size_t)tl * nkx * a.Hpad;
-    for (int e = tid; e < ny2 * nkx; e += nthr) {
-      const int k = lg2 >= 0 ? e >> lg2 : e / ny2;
-      const int yl = e - k * ny2;
-      const int p = yl >> 1;
+    for (int e = tid; e < np * nkx; e += nthr) {
+      const int k = lgp >= 0 ? e >> lgp : e / np;
+      const int p = e - k * np;
       const cx<S> zk = buf[swz<S>(p * ld + a.permx[k])];
       const cx<S> zn = buf[swz<S>(p * ld + a.permx[k == 0 ? 0 : nx - k])];
-      cx<S> v;
-      if ((yl & 1) == 0) {
-        v = {sc<S>::half(sc<S>::add(zk.r, zn.r)), sc<S>::half(sc<S>::sub(zk.i, zn.i))};
-      } else {
-        v = {sc<S>::half(sc<S>::add(zk.i, zn.i)), sc<S>::half(sc<S>::sub(zn.r, zk.r))};
-      }
-      R[(size_t)k * a.Hpad + 2 * pair0 + yl] = v;
+      cx<S>* dst = R + (size_t)k * a.Hpad + 2 * (pair0 + p);
+      dst[0] = {sc<S>::half(sc<S>::add(zk.r, zn.r)), sc<S>::half(sc<S>::sub(zk.i, zn.i))};
+      dst[1] = {sc<S>::half(sc<S>::add(zk.i, zn.i)), sc<S>::half(sc<S>::sub(zn.r, zk.r))};
     }
     b ^= 1;
   }
@@ -369,6 +364,34 @@ __device__ __forceinline__ void cols_issue(const SpatialArgs& a, int item, cx<S>
   cp_async_commit();
 }
 
+// Store phase of the column pass: scale by 1/sqrt(nx ny), apply the y-fftshift and
+// write F[q][t].  P2: the scale is a power of two and one multiply per word is exact.
+template <class S, bool P2>
+__device__ __forceinline__ void cols_store(const SpatialArgs& a, const cx<S>* buf, cx<S>* F, int ld, int kc0,
+                                           int tl0, int nk, int ntg, int lgTG, int lgCK, S norm, int tid,
+                                           int nthr) {
+  const int ny = a.ny, nkx = a.nkx, CK = a.cols_per_block, TG = a.frames_per_block;
+  const int half = ny >> 1;
+  for (int e = tid; e < CK * TG * ny; e += nthr) {
+    int tl, rest, kc, ky;
+    if (lgTG >= 0) { tl = e & (TG - 1); rest = e >> lgTG; } else { tl = e % TG; rest = e / TG; }
+    if (lgCK >= 0) { kc = rest & (CK - 1); ky = rest >> lgCK; } else { kc = rest % CK; ky = rest / CK; }
+    if (tl < ntg && kc < nk) {
+      const cx<S> z = buf[swz<S>((tl * CK + kc) * ld + a.permy[ky])];
+      cx<S> v;
+      if constexpr (P2) {
+        v = {sc<S>::mul_p2(z.r, a.norm_h), sc<S>::mul_p2(z.i, a.norm_h)};
+      } else {
+        v = cscale(z, norm);
+      }
+      int ys = ky + half;
+      if (ys >= ny) ys -= ny;
+      const size_t q = (size_t)ys * nkx + kc0 + kc;
+      F[q * a.Tpad + a.t0 + tl0 + tl] = v;
+    }
+  }
+}
+
 template <class S>
 __global__ void __launch_bounds__(512) k_cols(SpatialArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -382,8 +405,9 @@ __global__ void __launch_bounds__(512) k_cols(SpatialArgs a) {
   const int lgCK = (CK & (CK - 1)) == 0 ? __ffs(CK) - 1 : -1;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const S norm = sc<S>::cst(a.norm_h, a.norm_l, a.norm_d);
+  // 1/sqrt(nx ny) is a power of two when nx ny is a power of four: exact scaling
+  const bool norm_p2 = a.norm_l == 0.0f && (__float_as_uint(a.norm_h) & 0x007FFFFFu) == 0u;
   cx<S>* F = reinterpret_cast<cx<S>*>(a.spec);
-  const int half = ny >> 1;
   int b = 0;
   if ((int)blockIdx.x < nitems) cols_issue<S>(a, blockIdx.x, bufs[0], ncg, ld, tid, nthr);
 
@@ -396,18 +420,10 @@ __global__ void __launch_bounds__(512) k_cols(SpatialArgs a) {
     const int kc0 = (item % ncg) * CK, tl0 = (item / ncg) * TG;
     const int nk = min(CK, nkx - kc0), ntg = min(TG, a.tc - tl0);
     fft_forward<S>(buf, NB, ld, a.py, reinterpret_cast<const cx<S>*>(a.twy), tid, nthr);
-    for (int e = tid; e < NB * ny; e += nthr) {
-      int tl, rest, kc, ky;
-      if (lgTG >= 0) { tl = e & (TG - 1); rest = e >> lgTG; } else { tl = e % TG; rest = e / TG; }
-      if (lgCK >= 0) { kc = rest & (CK - 1); ky = rest >> lgCK; } else { kc = rest % CK; ky = rest / CK; }
-      if (tl < ntg && kc < nk) {
-        const cx<S> v = cscale(buf[swz<S>((tl * CK + kc) * ld + a.permy[ky])], norm);
-        int ys = ky + half;
-        if (ys >= ny) ys -= ny;
-        const size_t q = (size_t)ys * nkx + kc0 + kc;
-        F[q * a.Tpad + a.t0 + tl0 + tl] = v;
-      }
-    }
+    if (norm_p2)
+      cols_store<S, true>(a, buf, F, ld, kc0, tl0, nk, ntg, lgTG, lgCK, norm, tid, nthr);
+    else
+      cols_store<S, false>(a, buf, F, ld, kc0, tl0, nk, ntg, lgTG, lgCK, norm, tid, nthr);
     b ^= 1;
   }
 }

@@ -104,6 +104,8 @@ template <> struct sc<float> {
   static __device__ __forceinline__ double to_double(float a) { return (double)a; }
   // constant tables store (hi, lo) float pairs; FP32 uses hi only
   static __device__ __forceinline__ float cst(float h, float l, double d) { return h; }
+  // multiplication by a power of two (exact)
+  static __device__ __forceinline__ float mul_p2(float a, float p2) { return __fmul_rn(a, p2); }
 };
 
 template <> struct sc<ff> {
@@ -118,6 +120,7 @@ template <> struct sc<ff> {
   static __device__ __forceinline__ ff from_double(double a) { return ff_from_double(a); }
   static __device__ __forceinline__ double to_double(ff a) { return ff_to_double(a); }
   static __device__ __forceinline__ ff cst(float h, float l, double d) { return {h, l}; }
+  static __device__ __forceinline__ ff mul_p2(ff a, float p2) { return ff_scale2(a, p2); }
 };
 
 template <> struct sc<double> {
@@ -132,6 +135,7 @@ template <> struct sc<double> {
   static __device__ __forceinline__ double from_double(double a) { return a; }
   static __device__ __forceinline__ double to_double(double a) { return a; }
   static __device__ __forceinline__ double cst(float h, float l, double d) { return d; }
+  static __device__ __forceinline__ double mul_p2(double a, float p2) { return a * (double)p2; }
 };
 
 // Conversion between accumulation types (ff <-> double <-> float).
