@@ -66,6 +66,14 @@ cudaError_t dispatch_rows(int dtype, const SpatialArgs& a, int items, size_t sme
 // Returns 0 on success, else an FDDM status code with `err` filled in.
 template <class S, class A>
 int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
+  // the transform path pairs every lag with its prefix sums by position and
+  // sums the last lags directly from the end of the list
+  if (r.mode == MODE_FFT)
+    for (size_t l = 1; l < r.lags.size(); ++l)
+      if (r.lags[l] <= r.lags[l - 1]) {
+        err = "fft mode needs strictly increasing lags";
+        return 1;
+      }
   WorkLayout L;
   if (!plan_layout(r, L, err)) return 4;
   if (r.work_bytes < L.total) {

@@ -186,7 +186,9 @@ bool attach_pass_tables(FftPlan& p, int kind, std::string& err) {
   for (int s = 0; s < p.npass; ++s) {
     const int M = p.block[s], R = p.radix[s];
     p.ptw[s] = nullptr;
-    if (M / R <= 1) continue;
+    // stride-1 passes take no twiddles, except the first pass of a single-pass
+    // plan: the padded first pass reads its (all-ones) table unconditionally
+    if (M / R <= 1 && s > 0) continue;
     const auto& h = host_pass_table(M, R, kind);
     std::lock_guard<std::mutex> lk(g_pass_mu);
     auto key = std::make_tuple(dev, M, R, kind);
@@ -211,7 +213,7 @@ bool upload_pass_tables(FftPlan& p, int kind, unsigned char* dst, size_t room, c
   for (int s = 0; s < p.npass; ++s) {
     const int M = p.block[s], R = p.radix[s];
     p.ptw[s] = nullptr;
-    if (M / R <= 1) continue;
+    if (M / R <= 1 && s > 0) continue;  // as in attach_pass_tables
     const auto& h = host_pass_table(M, R, kind);  // cached: stays valid for the asynchronous copy
     if (used + up256(h.size()) > room) {
       err = "workspace table area too small for the pass twiddle tables";

@@ -81,7 +81,9 @@ int fddm_b200_workspace_size(int mode, int precision, uint64_t length, uint64_t 
 /* Image structure function, fft mode.  Replaces ddm_fft<T> (src/cpp/ddm.h:54-61,
    src/cpp/ddm.cc:250-453) and ddm_fft_cuda<T> (src/cuda/ddm_cuda.h:53).
      d_img_seq   (length, height, width) C-contiguous frames of `dtype`
-     lags        HOST array of nlags lags in [0, length-1] (the reference's vector<unsigned>)
+     lags        HOST array of nlags lags in [0, length-1] (the reference's vector<unsigned>);
+                 fft mode needs them strictly increasing, as the reference's fft core
+                 does (src/cpp/ddm.cc:403 matches them from the end), diff mode takes any order
      nx, ny      padded FFT sizes (>= width, height; factors 2,3,5,7,11,13)
      nt          the reference's temporal FFT length; must be >= 2*length-1.  Any
                  such length gives the same linear autocorrelation, so the library

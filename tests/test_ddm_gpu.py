@@ -171,6 +171,38 @@ def test_split_temporal_kernel(fddm, monkeypatch, T, split):
         _check(r._data, imgs, lags, "fft", precision, w, label=f"split {split} T={T}")
 
 
+@pytest.mark.parametrize("T", [1, 2, 3, 4, 5, 6, 8, 9])
+def test_tiny_sequences_fft(fddm, T):
+    """Very short series: single-pass temporal plans (T = 1, 2, 4), whose padded first
+    pass reads an all-ones twiddle table, and lags all in the direct tail."""
+    imgs = _poisson_stack((T, 6, 8), "uint16", seed=T)
+    lags = list(range(1, T))
+    for precision in ("ff", "f64"):
+        if T == 1:
+            with pytest.warns(UserWarning):
+                r = fddm.ddm(imgs, [0], mode="fft", precision=precision)
+        else:
+            r = fddm.ddm(imgs, lags, mode="fft", precision=precision)
+        _check(r._data, imgs, lags, "fft", precision, label=f"tiny T={T}")
+
+
+def test_lag_order_at_the_c_abi(fddm):
+    """fft mode needs strictly increasing lags (the transform path pairs them with
+    prefix sums by position and sums the last ones directly from the end of the
+    list); diff mode returns rows in the given order."""
+    from fastddm_gb300 import _ddm_b200
+    from fastddm_gb300._lib import FddmError
+
+    imgs = _poisson_stack((12, 8, 10), "uint16", seed=4)
+    with pytest.raises(FddmError, match="strictly increasing"):
+        _ddm_b200.ddm_device(imgs, [5, 1, 3], 10, 8, 32, mode="fft")
+    with pytest.raises(FddmError, match="strictly increasing"):
+        _ddm_b200.ddm_device(imgs, [1, 3, 3], 10, 8, 32, mode="fft")
+    got = _ddm_b200.ddm_device(imgs, [5, 1, 3], 10, 8, 0, mode="diff").cpu().numpy()
+    ex = _exact(imgs, [1, 3, 5])
+    np.testing.assert_allclose(got[[1, 2, 0]], ex[:3], rtol=1e-8, atol=1e-13 * np.abs(ex).max())
+
+
 @pytest.mark.parametrize("T,mode,precision", [
     (7000, "fft", "ff"),     # just past the single-CTA transform: split kernel
     (20000, "fft", "ff"),
