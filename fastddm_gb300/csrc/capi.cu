@@ -1,6 +1,7 @@
 // C ABI entry points (declared in include/fddm_b200.h).
 #include <atomic>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -76,7 +77,7 @@ void count_launches(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order
 
 namespace {
 std::mutex g_copy_mu;
-std::map<int, CopyCtx> g_copy;  // per device
+std::map<int, std::unique_ptr<CopyCtx>> g_copy;  // per device
 }  // namespace
 
 CopyCtx* copy_ctx(std::string& err) {
@@ -86,16 +87,16 @@ CopyCtx* copy_ctx(std::string& err) {
   std::lock_guard<std::mutex> lk(g_copy_mu);
   auto it = g_copy.find(dev);
   if (it == g_copy.end()) {
-    CopyCtx c{};
-    if ((ce = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking)) != cudaSuccess ||
-        (ce = cudaEventCreateWithFlags(&c.ready, cudaEventDisableTiming)) != cudaSuccess ||
-        (ce = cudaEventCreateWithFlags(&c.start, cudaEventDisableTiming)) != cudaSuccess) {
+    auto c = std::make_unique<CopyCtx>();
+    if ((ce = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (ce = cudaEventCreateWithFlags(&c->ready, cudaEventDisableTiming)) != cudaSuccess ||
+        (ce = cudaEventCreateWithFlags(&c->start, cudaEventDisableTiming)) != cudaSuccess) {
       err = cudaGetErrorString(ce);
       return nullptr;
     }
-    it = g_copy.emplace(dev, c).first;
+    it = g_copy.emplace(dev, std::move(c)).first;
   }
-  return &it->second;
+  return it->second.get();
 }
 
 size_t dtype_bytes(int dtype) {

@@ -207,6 +207,13 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   if ((ce = allow_smem(k_cols<S>, smem_cols)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
   CopyCtx* cp = nullptr;
   const size_t frame_bytes = (size_t)H * W * dtype_bytes(r.dtype);
+  // host frames or a host result: this call owns the device's copy events until it has enqueued everything
+  std::unique_lock<std::mutex> copy_lock;
+  if (r.host_img || r.host_out) {
+    CopyCtx* c = copy_ctx(err);
+    if (!c) return 3;
+    copy_lock = std::unique_lock<std::mutex>(c->mu);
+  }
   if (r.host_img) {
     if (!(cp = copy_ctx(err))) return 3;
     // the copies may only overwrite the frame buffer after earlier work on `st`

@@ -2,6 +2,7 @@
 #pragma once
 #include <stddef.h>
 #include <stdint.h>
+#include <mutex>
 #include <string>
 #include <vector>
 #include <cuda_runtime.h>
@@ -100,9 +101,13 @@ struct DdmRequest {
 };
 
 // Per-device copy stream and event used to overlap frame uploads with compute.
+// One per device: the events are re-recorded by every call, so a call holds
+// `mu` from its first record to its last wait (calls from several threads
+// would otherwise wait on each other's events).
 struct CopyCtx {
-  cudaStream_t stream;
-  cudaEvent_t ready, start;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ready = nullptr, start = nullptr;
+  std::mutex mu;
 };
 CopyCtx* copy_ctx(std::string& err);
 size_t dtype_bytes(int dtype);
