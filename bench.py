@@ -345,6 +345,28 @@ def run_ours(args):
                 "stage_ms": {"spatial": sp_ms, "temporal": tp_ms},
                 "job_bytes": job_bytes, "job_frac": job_bytes / (ms_step / 1000.0) / 1e9 / hbm}
 
+    # instruction-issue roofline: the float-float FFTs are bound by the SM issue rate (4 warp
+    # instructions per cycle per SM), not by HBM.  Warp instructions per mode / per frame come
+    # from an ncu capture of the same kernel configuration; the times and the clock are live.
+    issue = None
+    ifile = ROOT / "profiles" / "instructions.json"
+    if ifile.exists():
+        try:
+            ic = json.loads(ifile.read_text()).get(f"{args.config}:{args.mode}:{args.precision}")
+        except ValueError:
+            ic = None
+        mhz = clocks.get("sm_mhz") if isinstance(clocks, dict) else None
+        if ic and mhz:
+            cyc = torch.cuda.get_device_properties(device).multi_processor_count * mhz * 1e6
+            t_inst = ic["k_tfft_per_mode"] * Q
+            s_inst = (ic["k_rows_per_frame"] + ic["k_cols_per_frame"]) * T
+            t_rate = t_inst / (tp_ms / 1000.0) / cyc
+            issue = {"bound": "sm_issue", "kernel": "k_tfft", "achieved": t_rate, "peak": 4.0,
+                     "unit": "warp instructions/cycle/SM", "frac": t_rate / 4.0,
+                     "spatial_frac": s_inst / (sp_ms / 1000.0) / cyc / 4.0,
+                     "job_frac": (t_inst + s_inst) / (ms_step / 1000.0) / cyc / 4.0,
+                     "sm_mhz": mhz, "source": ic["source"]}
+
     # end to end through the public API: pinned host frames in, host result out
     e2e = None
     if not args.no_e2e and rank == 0:
@@ -384,7 +406,8 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": {"ff": "ff (float-float)", "f64": "f64", "f32": "f32"}[args.precision],
             "data": "synthetic", "config": workload_desc(args.config, scene, lags, args.precision, args.mode),
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
+            "roofline": roofline, "issue_roofline": issue, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": launches,
         }
         print(json.dumps(line))
     if ws > 1:
