@@ -241,7 +241,7 @@ __device__ __forceinline__ void rows_issue_raw(const SpatialArgs& a, int item, u
   cp_async_commit();
 }
 
-template <class S, class IN>
+template <class S, class IN, bool P2>
 __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
       buf[swz<S>(p * ld + x)] = {va, vb};
     }
     __syncthreads();
-    fft_forward<S>(buf, np, ld, a.px, reinterpret_cast<const cx<S>*>(a.twx), tid, nthr);
+    fft_forward<S, P2>(buf, np, ld, a.px, reinterpret_cast<const cx<S>*>(a.twx), tid, nthr);
 
     // unpack Z = A + iB into the spectra of the two real rows of each pair,
     // one thread per (k, pair): R[tl][k][2p] and R[tl][k][2p + 1]
@@ -392,7 +392,7 @@ __device__ __forceinline__ void cols_store(const SpatialArgs& a, const cx<S>* bu
   }
 }
 
-template <class S>
+template <class S, bool P2>
 __global__ void __launch_bounds__(512) k_cols(SpatialArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int ny = a.ny, nkx = a.nkx;
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(512) k_cols(SpatialArgs a) {
     cx<S>* buf = bufs[b];
     const int kc0 = (item % ncg) * CK, tl0 = (item / ncg) * TG;
     const int nk = min(CK, nkx - kc0), ntg = min(TG, a.tc - tl0);
-    fft_forward<S>(buf, NB, ld, a.py, reinterpret_cast<const cx<S>*>(a.twy), tid, nthr);
+    fft_forward<S, P2>(buf, NB, ld, a.py, reinterpret_cast<const cx<S>*>(a.twy), tid, nthr);
     if (norm_p2)
       cols_store<S, true>(a, buf, F, ld, kc0, tl0, nk, ntg, lgTG, lgCK, norm, tid, nthr);
     else
@@ -494,7 +494,7 @@ __device__ __forceinline__ void pair_power(cx<S>* __restrict__ buf, int M1, int 
   }
 }
 
-template <class S, class A>
+template <class S, class A, bool P2>
 __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int T = a.T, N = a.nt, N2 = a.nt / 2, nl = a.nlags;
@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
     if (tid == 0 && slotB[0] >= 0) need[nl + slotB[0]] = sc<A>::zero();
     __syncthreads();
 
-    fft_forward_padded<S>(buf, a.pt, T, tw, tid, nthr);
+    fft_forward_padded<S, P2>(buf, a.pt, T, tw, tid, nthr);
     if (R0 == 8) pair_power<S, 8>(buf, M1, tid, nthr);
     else if (R0 == 4) pair_power<S, 4>(buf, M1, tid, nthr);
     else pair_power<S, 2>(buf, M1, tid, nthr);
@@ -607,7 +607,7 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
     // buf above the half-length transform is free: start loading the next mode
     if (q + gridDim.x < a.q_end) prefetch_series<S>(ser, F + (q + gridDim.x) * a.Tpad, T, tid, nthr);
     // the length-N table serves the half-length passes: w_M^k = tw[k N / M]
-    fft_inverse<S>(buf, 1, N2, a.pt2, tw, tid, nthr, N);
+    fft_inverse<S, P2>(buf, 1, N2, a.pt2, tw, tid, nthr, N);
 
     total = scratch[32];
     for (int l = tid; l < nl; l += nthr) {

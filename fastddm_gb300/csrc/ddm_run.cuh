@@ -41,12 +41,25 @@ template <class K> inline unsigned persistent_grid(K kernel, int threads, size_t
   return (unsigned)std::max(1, std::min(items, std::max(occ, 1) * nsm));
 }
 
+// True when every pass of `p` has radix 2, 4 or 8: the kernels' P2 variants
+// then carry only those butterflies.
+inline bool plan_is_p2(const FftPlan& p) {
+  for (int s = 0; s < p.npass; ++s)
+    if (p.radix[s] != 2 && p.radix[s] != 4 && p.radix[s] != 8) return false;
+  return true;
+}
+
+template <class S, class IN, bool P2>
+cudaError_t launch_rows(const SpatialArgs& a, int items, size_t smem, cudaStream_t st) {
+  cudaError_t e = allow_smem(k_rows<S, IN, P2>, smem);
+  if (e != cudaSuccess) return e;
+  k_rows<S, IN, P2><<<persistent_grid(k_rows<S, IN, P2>, 256, smem, items), 256, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
 template <class S, class IN>
 cudaError_t launch_rows(const SpatialArgs& a, int items, size_t smem, cudaStream_t st) {
-  cudaError_t e = allow_smem(k_rows<S, IN>, smem);
-  if (e != cudaSuccess) return e;
-  k_rows<S, IN><<<persistent_grid(k_rows<S, IN>, 256, smem, items), 256, smem, st>>>(a);
-  return cudaGetLastError();
+  return plan_is_p2(a.px) ? launch_rows<S, IN, true>(a, items, smem, st) : launch_rows<S, IN, false>(a, items, smem, st);
 }
 
 template <class S>
@@ -204,7 +217,11 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   const size_t smem_rows = (size_t)swz_round<S>(L.pairs_per_block * (nx + G)) * sizeof(cx<S>) + 2 * (size_t)sa.raw_stage_bytes;
   const size_t smem_cols = 2 * (size_t)swz_round<S>(L.cols_per_block * L.frames_per_block * (ny + G)) * sizeof(cx<S>);
   const int ngroups = (npairs + L.pairs_per_block - 1) / L.pairs_per_block;
-  if ((ce = allow_smem(k_cols<S>, smem_cols)) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
+  const bool p2y = plan_is_p2(sa.py);
+  if ((ce = p2y ? allow_smem(k_cols<S, true>, smem_cols) : allow_smem(k_cols<S, false>, smem_cols)) != cudaSuccess) {
+    err = cudaGetErrorString(ce);
+    return 3;
+  }
   CopyCtx* cp = nullptr;
   const size_t frame_bytes = (size_t)H * W * dtype_bytes(r.dtype);
   // host frames or a host result: this call owns the device's copy events until it has enqueued everything
@@ -242,7 +259,8 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     }
     const int col_items = ((nkx + L.cols_per_block - 1) / L.cols_per_block) *
                           ((sa.tc + L.frames_per_block - 1) / L.frames_per_block);
-    k_cols<S><<<persistent_grid(k_cols<S>, 512, smem_cols, col_items), 512, smem_cols, st>>>(sa);
+    if (p2y) k_cols<S, true><<<persistent_grid(k_cols<S, true>, 512, smem_cols, col_items), 512, smem_cols, st>>>(sa);
+    else k_cols<S, false><<<persistent_grid(k_cols<S, false>, 512, smem_cols, col_items), 512, smem_cols, st>>>(sa);
     if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
     launches += 2;
   }
@@ -287,6 +305,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   } else if (!L.diff_staged) {
     smem_t = 96 * sizeof(A);
   }
+  const bool p2t = r.mode == MODE_FFT && !long_fft && plan_is_p2(ta.pt) && plan_is_p2(ta.pt2);
   ta.lags = d_lags; ta.rcp = d_rcp; ta.out = r.out;
   split_ff(1.0 / (double)T, ta.invT_h, ta.invT_l); ta.invT_d = 1.0 / (double)T;
   int dev = 0, nsm = 0, occ = 0;
@@ -299,7 +318,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   };
   bool prepared;
   if (long_fft) prepared = prepare(k_tfft_long<S, A>);
-  else if (r.mode == MODE_FFT) prepared = prepare(k_tfft<S, A>);
+  else if (r.mode == MODE_FFT) prepared = p2t ? prepare(k_tfft<S, A, true>) : prepare(k_tfft<S, A, false>);
   else if (L.diff_staged) prepared = prepare(k_tdiff<S, A, true>);
   else prepared = prepare(k_tdiff<S, A, false>);
   if (!prepared) return 3;
@@ -317,7 +336,8 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     const unsigned grid = (unsigned)std::min<size_t>(ta.q_end - ta.q_begin, max_grid);
     if (grid == 0) continue;
     if (long_fft) k_tfft_long<S, A><<<grid, threads, smem_t, st>>>(ta);
-    else if (r.mode == MODE_FFT) k_tfft<S, A><<<grid, threads, smem_t, st>>>(ta);
+    else if (r.mode == MODE_FFT && p2t) k_tfft<S, A, true><<<grid, threads, smem_t, st>>>(ta);
+    else if (r.mode == MODE_FFT) k_tfft<S, A, false><<<grid, threads, smem_t, st>>>(ta);
     else if (L.diff_staged) k_tdiff<S, A, true><<<grid, threads, smem_t, st>>>(ta);
     else k_tdiff<S, A, false><<<grid, threads, smem_t, st>>>(ta);
     if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }

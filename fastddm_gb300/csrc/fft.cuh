@@ -216,21 +216,29 @@ __device__ __forceinline__ void fft_pass(cx<S>* __restrict__ buf, int nfft, int 
   }
 }
 
-template <class S, bool INV>
+// P2: the plan's radices are all 2, 4 or 8 (plan_is_p2), so the other
+// butterflies are not compiled into the caller (smaller code, fewer registers).
+template <class S, bool INV, bool P2 = false>
 __device__ __forceinline__ void fft_pass_dispatch(cx<S>* buf, int nfft, int ld, const FftPlan& p, int s,
                                                   const cx<S>* tw, int twn, int tid, int nthr) {
   const int n = p.n, M = p.block[s], lgs = p.lgstride[s], lgb = p.lgbpf[s];
   const cx<S>* ptw = reinterpret_cast<const cx<S>*>(p.ptw[s]);
   switch (p.radix[s]) {
     case 2: fft_pass<S, 2, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
-    case 3: fft_pass<S, 3, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
     case 4: fft_pass<S, 4, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
-    case 5: fft_pass<S, 5, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
-    case 7: fft_pass<S, 7, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
     case 8: fft_pass<S, 8, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
-    case 11: fft_pass<S, 11, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
-    case 13: fft_pass<S, 13, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
-    default: break;
+    default:
+      if constexpr (!P2) {
+        switch (p.radix[s]) {
+          case 3: fft_pass<S, 3, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
+          case 5: fft_pass<S, 5, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
+          case 7: fft_pass<S, 7, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
+          case 11: fft_pass<S, 11, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
+          case 13: fft_pass<S, 13, INV>(buf, nfft, ld, n, M, lgs, lgb, tw, twn, ptw, tid, nthr); break;
+          default: break;
+        }
+      }
+      break;
   }
 }
 
@@ -279,7 +287,7 @@ __device__ __forceinline__ void fft_first_pass_padded(cx<S>* __restrict__ buf, c
 }
 
 // Forward transform of a zero-padded input (zeros at indices >= limit, limit <= n/2).
-template <class S>
+template <class S, bool P2 = false>
 __device__ void fft_forward_padded(cx<S>* buf, const FftPlan& p, int limit, const cx<S>* tw, int tid, int nthr) {
   switch (p.radix[0]) {
     case 2: fft_first_pass_padded<S, 2>(buf, p, limit, tw, tid, nthr); break;
@@ -288,12 +296,12 @@ __device__ void fft_forward_padded(cx<S>* buf, const FftPlan& p, int limit, cons
     default:  // odd first radix (plans for the temporal transform start with 2, 4 or 8): zero-fill, full pass
       for (int i = limit + tid; i < p.n; i += nthr) buf[swz<S>(i)] = czero<S>();
       __syncthreads();
-      fft_pass_dispatch<S, false>(buf, 1, p.n, p, 0, tw, p.n, tid, nthr);
+      fft_pass_dispatch<S, false, P2>(buf, 1, p.n, p, 0, tw, p.n, tid, nthr);
       break;
   }
   __syncthreads();
   for (int s = 1; s < p.npass; ++s) {
-    fft_pass_dispatch<S, false>(buf, 1, p.n, p, s, tw, p.n, tid, nthr);
+    fft_pass_dispatch<S, false, P2>(buf, 1, p.n, p, s, tw, p.n, tid, nthr);
     __syncthreads();
   }
 }
@@ -301,23 +309,23 @@ __device__ void fft_forward_padded(cx<S>* buf, const FftPlan& p, int limit, cons
 // Forward DIF: natural order in, digit-reversed (perm) order out.
 // Caller synchronises before the call; the function ends with a barrier.
 // twn: length of the twiddle table `tw` (0: p.n).
-template <class S>
+template <class S, bool P2 = false>
 __device__ void fft_forward(cx<S>* buf, int nfft, int ld, const FftPlan& p, const cx<S>* tw, int tid,
                             int nthr, int twn = 0) {
   if (twn == 0) twn = p.n;
   for (int s = 0; s < p.npass; ++s) {
-    fft_pass_dispatch<S, false>(buf, nfft, ld, p, s, tw, twn, tid, nthr);
+    fft_pass_dispatch<S, false, P2>(buf, nfft, ld, p, s, tw, twn, tid, nthr);
     __syncthreads();
   }
 }
 
 // Inverse (unnormalised, sum_k X_k w^(-jk)): perm order in, natural order out.
-template <class S>
+template <class S, bool P2 = false>
 __device__ void fft_inverse(cx<S>* buf, int nfft, int ld, const FftPlan& p, const cx<S>* tw, int tid,
                             int nthr, int twn = 0) {
   if (twn == 0) twn = p.n;
   for (int s = p.npass - 1; s >= 0; --s) {
-    fft_pass_dispatch<S, true>(buf, nfft, ld, p, s, tw, twn, tid, nthr);
+    fft_pass_dispatch<S, true, P2>(buf, nfft, ld, p, s, tw, twn, tid, nthr);
     __syncthreads();
   }
 }
