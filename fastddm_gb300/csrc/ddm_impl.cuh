@@ -495,7 +495,7 @@ __device__ __forceinline__ void pair_power(cx<S>* __restrict__ buf, int M1, int 
 }
 
 template <class S, class A, bool P2>
-__global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
+__device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int T = a.T, N = a.nt, N2 = a.nt / 2, nl = a.nlags;
   cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
@@ -648,6 +648,16 @@ __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
 #undef FDDM_LAG_W
 #undef FDDM_LAG_RCP
 #undef FDDM_LAG_TAU
+}
+
+template <class S, class A, bool P2>
+__global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
+  tfft_body<S, A, P2>(a);
+}
+// FP32 transforms: two 512-thread CTAs per SM (their shared memory allows it)
+template <class S, class A, bool P2>
+__global__ void __launch_bounds__(512, 2) k_tfft_x2(TemporalArgs a) {
+  tfft_body<S, A, P2>(a);
 }
 
 // ---------------------------------------------------------------------------

@@ -49,6 +49,12 @@ inline bool plan_is_p2(const FftPlan& p) {
   return true;
 }
 
+// Temporal kernel of a tier: FP32 transforms run two CTAs per SM.
+template <class S, class A, bool P2> constexpr auto tfft_kernel() {
+  if constexpr (sizeof(S) == 4) return &k_tfft_x2<S, A, P2>;
+  else return &k_tfft<S, A, P2>;
+}
+
 template <class S, class IN, bool P2>
 cudaError_t launch_rows(const SpatialArgs& a, int items, size_t smem, cudaStream_t st) {
   cudaError_t e = allow_smem(k_rows<S, IN, P2>, smem);
@@ -318,7 +324,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   };
   bool prepared;
   if (long_fft) prepared = prepare(k_tfft_long<S, A>);
-  else if (r.mode == MODE_FFT) prepared = p2t ? prepare(k_tfft<S, A, true>) : prepare(k_tfft<S, A, false>);
+  else if (r.mode == MODE_FFT) prepared = p2t ? prepare(tfft_kernel<S, A, true>()) : prepare(tfft_kernel<S, A, false>());
   else if (L.diff_staged) prepared = prepare(k_tdiff<S, A, true>);
   else prepared = prepare(k_tdiff<S, A, false>);
   if (!prepared) return 3;
@@ -336,8 +342,8 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     const unsigned grid = (unsigned)std::min<size_t>(ta.q_end - ta.q_begin, max_grid);
     if (grid == 0) continue;
     if (long_fft) k_tfft_long<S, A><<<grid, threads, smem_t, st>>>(ta);
-    else if (r.mode == MODE_FFT && p2t) k_tfft<S, A, true><<<grid, threads, smem_t, st>>>(ta);
-    else if (r.mode == MODE_FFT) k_tfft<S, A, false><<<grid, threads, smem_t, st>>>(ta);
+    else if (r.mode == MODE_FFT && p2t) tfft_kernel<S, A, true>()<<<grid, threads, smem_t, st>>>(ta);
+    else if (r.mode == MODE_FFT) tfft_kernel<S, A, false>()<<<grid, threads, smem_t, st>>>(ta);
     else if (L.diff_staged) k_tdiff<S, A, true><<<grid, threads, smem_t, st>>>(ta);
     else k_tdiff<S, A, false><<<grid, threads, smem_t, st>>>(ta);
     if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
