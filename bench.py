@@ -8,7 +8,9 @@ autocorrelation, combination); the stack (4.2 GB) and the spectrum (34 GB) are
 far larger than L2, so no flush is needed between steps.
 
 Prints one JSON line (rank 0).  ``--impl reference`` times the CPU restatement
-of the reference's FP64 core on the host cores instead.
+of the reference's FP64 core on all host cores instead (the reference's own
+``cpp`` core needs its CMake build and cannot be compiled from its sources
+alone).
 """
 
 from __future__ import annotations

@@ -40,7 +40,7 @@ extern "C" {
 #define FDDM_ERR_INVALID 1     /* bad argument (sizes, lags, dtype, null pointer) */
 #define FDDM_ERR_NOMEM 2       /* workspace too small / device allocation failed */
 #define FDDM_ERR_CUDA 3        /* a CUDA runtime call or kernel launch failed */
-#define FDDM_ERR_UNSUPPORTED 4 /* valid input this build cannot process (e.g. T too long) */
+#define FDDM_ERR_UNSUPPORTED 4 /* valid input the library cannot process (e.g. T too long) */
 
 /* input pixel types: the nine dtypes the reference binds (ddm_bindings.h:25-43).
    64-bit integers are converted to double by the caller, as the reference's
