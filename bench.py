@@ -190,10 +190,9 @@ class ClockSampler:
 
 # ---------------------------------------------------------------------------
 def dist_setup():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from fastddm_gb300 import replicas
+
+    return replicas.world()
 
 
 def run_reference(args):
@@ -249,7 +248,7 @@ def run_ours(args):
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
 
-    from fastddm_gb300 import _build, _lib, synthetic, window as fwin
+    from fastddm_gb300 import _build, _lib, replicas, synthetic, window as fwin
     from fastddm_gb300._ddm_b200 import DdmPlan, ddm_fft_b200
     from fastddm_gb300._fftopt import next_fast_len
 
@@ -279,24 +278,18 @@ def run_ours(args):
     launches0 = lib.fddm_b200_launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(torch.cuda.current_device()) as clk:
-        if ws > 1:
-            torch.distributed.barrier()
+        replicas.barrier()
         torch.cuda.synchronize(device)
         e0.record(stream)
         for _ in range(args.steps):
             plan.run(frames, window, out, stream)
         e1.record(stream)
         torch.cuda.synchronize(device)
-        if ws > 1:
-            torch.distributed.barrier()
+        replicas.barrier()
     launches = int(lib.fddm_b200_launch_count() - launches0)
-    ms = e0.elapsed_time(e1)
-    if ws > 1:
-        t = torch.tensor([ms], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(e0.elapsed_time(e1), device)
     ms_step = ms / args.steps
-    value = ws * T * args.steps / (ms / 1000.0)
+    value = replicas.aggregate_rate(T * args.steps, ms / 1000.0, ws)
     clocks = clk.summary()
 
     # per-stage device times (untimed extra steps with CUDA events around each stage)
