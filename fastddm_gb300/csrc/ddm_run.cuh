@@ -2,6 +2,7 @@
 #pragma once
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <string>
 #include "ddm_impl.cuh"
 
@@ -186,9 +187,25 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   if (evs) cudaEventRecord(evs->ev[0], st);
   int launches = r.window ? 1 : 0;
 
+  // Page-locked host frames that the device can address (mapped under unified
+  // addressing; NVLink-C2C on Grace parts) are read in place by the row pass:
+  // no copy-engine upload, no staging.  Pageable frames are uploaded chunk by
+  // chunk on the copy stream.  FDDM_B200_ZERO_COPY=0 forces the upload.
+  const void* host_direct = nullptr;
+  if (r.host_img) {
+    const char* zc = std::getenv("FDDM_B200_ZERO_COPY");
+    cudaPointerAttributes pa{};
+    if (!(zc && zc[0] == '0') && cudaPointerGetAttributes(&pa, r.host_img) == cudaSuccess &&
+        pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr)
+      host_direct = pa.devicePointer;
+    else
+      (void)cudaGetLastError();  // pageable memory reports an error here: clear it
+  }
+  const bool upload = r.host_img != nullptr && host_direct == nullptr;
+
   // stages 1-2 over frame chunks
   SpatialArgs sa{};
-  sa.img = r.img;
+  sa.img = host_direct ? host_direct : r.img;
   sa.window_s = win_s;
   sa.T = T; sa.H = H; sa.W = W; sa.nx = nx; sa.ny = ny; sa.nkx = nkx; sa.Hpad = L.Hpad;
   sa.Tpad = L.Tpad;
@@ -217,7 +234,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   // raw rows staged asynchronously when every row starts on a 16-byte boundary
   const size_t row_bytes = (size_t)W * dtype_bytes(r.dtype);
   const size_t stage = (size_t)2 * L.pairs_per_block * row_bytes;
-  sa.raw_stage_bytes = (row_bytes % 16 == 0 && (reinterpret_cast<uintptr_t>(r.img) % 16) == 0 && 2 * stage <= 64 * 1024)
+  sa.raw_stage_bytes = (row_bytes % 16 == 0 && (reinterpret_cast<uintptr_t>(sa.img) % 16) == 0 && 2 * stage <= 64 * 1024)
                            ? (int)stage : 0;
   const int G = swz_group<S>::G;
   const size_t smem_rows = (size_t)swz_round<S>(L.pairs_per_block * (nx + G)) * sizeof(cx<S>) + 2 * (size_t)sa.raw_stage_bytes;
@@ -232,12 +249,12 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   const size_t frame_bytes = (size_t)H * W * dtype_bytes(r.dtype);
   // host frames or a host result: this call owns the device's copy events until it has enqueued everything
   std::unique_lock<std::mutex> copy_lock;
-  if (r.host_img || r.host_out) {
+  if (upload || r.host_out) {
     CopyCtx* c = copy_ctx(err);
     if (!c) return 3;
     copy_lock = std::unique_lock<std::mutex>(c->mu);
   }
-  if (r.host_img) {
+  if (upload) {
     if (!(cp = copy_ctx(err))) return 3;
     // the copies may only overwrite the frame buffer after earlier work on `st`
     if ((ce = cudaEventRecord(cp->start, st)) != cudaSuccess || (ce = cudaStreamWaitEvent(cp->stream, cp->start, 0)) != cudaSuccess) {
@@ -248,7 +265,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   for (int t0 = 0; t0 < T; t0 += L.chunk) {
     sa.t0 = t0;
     sa.tc = std::min(L.chunk, T - t0);
-    if (r.host_img) {
+    if (upload) {
       const size_t off = (size_t)t0 * frame_bytes, n = (size_t)sa.tc * frame_bytes;
       if ((ce = cudaMemcpyAsync(static_cast<unsigned char*>(const_cast<void*>(r.img)) + off,
                                 static_cast<const unsigned char*>(r.host_img) + off, n, cudaMemcpyHostToDevice,

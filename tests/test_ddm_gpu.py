@@ -321,6 +321,22 @@ def test_backend_function_contract(fddm):
 
 
 @pytest.mark.parametrize("mode", ["fft", "diff"])
+def test_page_locked_frames_read_in_place_or_uploaded(fddm, monkeypatch, mode):
+    """Page-locked host frames are read by the row pass in place (no copy-engine upload);
+    FDDM_B200_ZERO_COPY=0 uploads them chunk by chunk instead: identical results."""
+    import torch
+
+    imgs = _poisson_stack((40, 72, 64), "uint8", seed=21, level=30.0)
+    lags = [1, 2, 5, 13, 39]
+    pinned = torch.from_numpy(imgs).pin_memory()
+    direct = fddm.ddm(pinned, lags, mode=mode)._data
+    monkeypatch.setenv("FDDM_B200_ZERO_COPY", "0")
+    uploaded = fddm.ddm(pinned, lags, mode=mode)._data
+    np.testing.assert_array_equal(direct, uploaded)
+    _check(direct, imgs, lags, mode, "ff", label="page-locked in place")
+
+
+@pytest.mark.parametrize("mode", ["fft", "diff"])
 def test_input_paths_agree(fddm, mode):
     """Pageable numpy, page-locked CPU tensor (overlapped upload) and CUDA tensor inputs give identical results."""
     import torch
