@@ -107,13 +107,16 @@ int fddm_b200_ddm_diff(const void* d_img_seq, int dtype, uint64_t length, uint64
                        const double* d_window, double* d_out, void* d_workspace, size_t workspace_bytes,
                        int precision, void* stream);
 
-/* Image structure function from frames in HOST memory, with the upload
-   overlapped with the computation (the reference's cores take host arrays:
-   src/cpp/ddm.h:38-61).  The frames are copied chunk by chunk from h_img_seq
-   into the caller's device buffer d_frames (length*height*width elements) on a
-   library copy stream; each chunk's spatial FFTs wait only for that chunk.  With
-   page-locked host memory the copies run concurrently with the kernels.  If
-   h_out is not NULL the result is also copied to it on `stream` at the end.
+/* Image structure function from frames in HOST memory (the reference's cores
+   take host arrays: src/cpp/ddm.h:38-61).  Page-locked frames (mapped into the
+   device's address space under unified addressing) are read in place by the
+   spatial kernels, over NVLink-C2C on Grace parts, and d_frames is not
+   touched.  Pageable frames (or FDDM_B200_ZERO_COPY=0 in the environment) are
+   copied chunk by chunk from h_img_seq into the caller's device buffer
+   d_frames (length*height*width elements) on a library copy stream; each
+   chunk's spatial FFTs wait only for that chunk.  If h_out is not NULL the
+   result is also copied to it, in column chunks overlapped with the temporal
+   stage.
    mode is FDDM_MODE_FFT or FDDM_MODE_DIFF (nt ignored for diff); the other
    arguments as fddm_b200_ddm_fft.  The host buffers must stay valid until the
    work on `stream` has completed. */
