@@ -9,7 +9,7 @@ messages and argument assembly, and the same axes:
 
 with I~ the 2D FFT of a frame divided by sqrt(nx * ny).  The registry holds
 the GB300 core ``'b200'``; the reference's ``_backend`` can register the same
-two functions (see ``INTEGRATION.md``).
+two functions, ``ddm_fft_b200`` and ``ddm_diff_b200``, under that key.
 """
 
 from __future__ import annotations
