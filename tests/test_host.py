@@ -108,6 +108,20 @@ def test_workspace_query_and_errors(built_lib):
     assert rc == _lib.FDDM_ERR_INVALID
 
 
+def test_fft_lags_must_increase(built_lib):
+    """fft mode refuses non-increasing lags before any device work (the arguments are
+    checked on the host, so dummy device pointers are never touched)."""
+    from fastddm_gb300 import _lib
+
+    dummy = ctypes.c_void_p(256)
+    for lags in ([5, 1, 3], [1, 3, 3]):
+        arr = (ctypes.c_uint32 * len(lags))(*lags)
+        rc = built_lib.fddm_b200_ddm_fft(dummy, 0, 8, 16, 16, arr, len(lags), 16, 16, 16, None, dummy, dummy,
+                                         1 << 20, 0, None)
+        assert rc == _lib.FDDM_ERR_INVALID
+        assert b"strictly increasing" in built_lib.fddm_b200_last_error()
+
+
 def test_status_to_exception(built_lib):
     from fastddm_gb300 import _lib
 
