@@ -187,30 +187,21 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   if (evs) cudaEventRecord(evs->ev[0], st);
   int launches = r.window ? 1 : 0;
 
-  // Host frames the device can address are read in place by the row pass (no
-  // copy-engine upload, no staging): page-locked memory, mapped under unified
-  // addressing, and pageable memory on devices that reach it through the host
-  // page tables (ATS on Grace parts, over NVLink-C2C).  Other pageable frames
-  // are uploaded chunk by chunk on the copy stream.  FDDM_B200_ZERO_COPY=0
-  // forces the upload.
+  // Page-locked host frames (mapped into the device's address space under
+  // unified addressing; NVLink-C2C on Grace parts) are read in place by the row
+  // pass: no copy-engine upload, no staging.  Pageable frames are uploaded chunk
+  // by chunk on the copy stream: they may be views of memory-mapped files whose
+  // pages are not resident, which the kernels must not read directly.
+  // FDDM_B200_ZERO_COPY=0 forces the upload for page-locked frames too.
   const void* host_direct = nullptr;
   if (r.host_img) {
     const char* zc = std::getenv("FDDM_B200_ZERO_COPY");
-    if (!(zc && zc[0] == '0')) {
-      cudaPointerAttributes pa{};
-      int dev = 0, ats = 0;
-      if (cudaPointerGetAttributes(&pa, r.host_img) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
-          pa.devicePointer != nullptr) {
-        host_direct = pa.devicePointer;
-      } else {
-        (void)cudaGetLastError();  // some runtimes report pageable memory as an error: clear it
-        if (pa.type != cudaMemoryTypeDevice && pa.type != cudaMemoryTypeManaged && cudaGetDevice(&dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) == cudaSuccess &&
-            ats == 1)
-          host_direct = r.host_img;
-        (void)cudaGetLastError();
-      }
-    }
+    cudaPointerAttributes pa{};
+    if (!(zc && zc[0] == '0') && cudaPointerGetAttributes(&pa, r.host_img) == cudaSuccess &&
+        pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr)
+      host_direct = pa.devicePointer;
+    else
+      (void)cudaGetLastError();  // some runtimes report pageable memory as an error: clear it
   }
   const bool upload = r.host_img != nullptr && host_direct == nullptr;
 

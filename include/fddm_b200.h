@@ -108,13 +108,12 @@ int fddm_b200_ddm_diff(const void* d_img_seq, int dtype, uint64_t length, uint64
                        int precision, void* stream);
 
 /* Image structure function from frames in HOST memory (the reference's cores
-   take host arrays: src/cpp/ddm.h:38-61).  Frames the device can address are
-   read in place by the spatial kernels and d_frames is not touched:
-   page-locked memory (mapped under unified addressing) and, on devices that
-   reach pageable memory through the host page tables (ATS over NVLink-C2C on
-   Grace parts), any host memory.  Otherwise (or with FDDM_B200_ZERO_COPY=0 in
-   the environment) the frames are copied chunk by chunk from h_img_seq into
-   the caller's device buffer
+   take host arrays: src/cpp/ddm.h:38-61).  Page-locked frames (mapped into
+   the device's address space under unified addressing) are read in place by
+   the spatial kernels, over NVLink-C2C on Grace parts, and d_frames is not
+   touched.  Pageable frames (or any, with FDDM_B200_ZERO_COPY=0 in the
+   environment) are copied chunk by chunk from h_img_seq into the caller's
+   device buffer
    d_frames (length*height*width elements) on a library copy stream; each
    chunk's spatial FFTs wait only for that chunk.  If h_out is not NULL the
    result is also copied to it, in column chunks overlapped with the temporal
