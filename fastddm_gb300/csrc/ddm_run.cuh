@@ -192,13 +192,21 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   // pass: no copy-engine upload, no staging.  Pageable frames are uploaded chunk
   // by chunk on the copy stream: they may be views of memory-mapped files whose
   // pages are not resident, which the kernels must not read directly.
-  // FDDM_B200_ZERO_COPY=0 forces the upload for page-locked frames too.
+  // In-place reads also need the row pass's staged path (16-byte aligned rows,
+  // fetched with cp.async ahead of use): its per-pixel fallback would wait on
+  // every host read.  FDDM_B200_ZERO_COPY=0 forces the upload for page-locked
+  // frames too.
+  const size_t row_bytes = (size_t)W * dtype_bytes(r.dtype);
+  const size_t stage = (size_t)2 * L.pairs_per_block * row_bytes;
+  auto stageable = [&](const void* p) {
+    return row_bytes % 16 == 0 && (reinterpret_cast<uintptr_t>(p) % 16) == 0 && 2 * stage <= 64 * 1024;
+  };
   const void* host_direct = nullptr;
   if (r.host_img) {
     const char* zc = std::getenv("FDDM_B200_ZERO_COPY");
     cudaPointerAttributes pa{};
     if (!(zc && zc[0] == '0') && cudaPointerGetAttributes(&pa, r.host_img) == cudaSuccess &&
-        pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr)
+        pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr && stageable(pa.devicePointer))
       host_direct = pa.devicePointer;
     else
       (void)cudaGetLastError();  // some runtimes report pageable memory as an error: clear it
@@ -234,10 +242,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   sa.norm_d = norm;
   const int npairs = (H + 1) / 2;
   // raw rows staged asynchronously when every row starts on a 16-byte boundary
-  const size_t row_bytes = (size_t)W * dtype_bytes(r.dtype);
-  const size_t stage = (size_t)2 * L.pairs_per_block * row_bytes;
-  sa.raw_stage_bytes = (row_bytes % 16 == 0 && (reinterpret_cast<uintptr_t>(sa.img) % 16) == 0 && 2 * stage <= 64 * 1024)
-                           ? (int)stage : 0;
+  sa.raw_stage_bytes = stageable(sa.img) ? (int)stage : 0;
   const int G = swz_group<S>::G;
   const size_t smem_rows = (size_t)swz_round<S>(L.pairs_per_block * (nx + G)) * sizeof(cx<S>) + 2 * (size_t)sa.raw_stage_bytes;
   const size_t smem_cols = 2 * (size_t)swz_round<S>(L.cols_per_block * L.frames_per_block * (ny + G)) * sizeof(cx<S>);
