@@ -193,6 +193,9 @@ class DdmPlan:
 
         `host` must stay alive until the stream has finished; `host_out`, if
         given, receives the result (page-locked memory makes the copy async).
+        `frames_dev` may be None for page-locked frames the row pass reads in
+        place; the library refuses that (FDDM_ERR_INVALID, nothing queued) when
+        they cannot be read in place.
         """
         lib = _lib.load()
         if stream is None:
@@ -205,7 +208,8 @@ class DdmPlan:
         with torch.cuda.device(self.device):
             code = lib.fddm_b200_ddm_from_host(
                 _lib.MODE[self.mode], _host_ptr(host), self.dtype_code, self.length, self.height, self.width,
-                lags_p, len(self._lags_c), self.nx, self.ny, self.nt, frames_dev.data_ptr(), wptr, out.data_ptr(),
+                lags_p, len(self._lags_c), self.nx, self.ny, self.nt,
+                frames_dev.data_ptr() if frames_dev is not None else None, wptr, out.data_ptr(),
                 hout, self.workspace.data_ptr(), self.workspace_bytes, _lib.PREC[self.precision], stream.cuda_stream,
             )
         _lib.check(code)
@@ -229,8 +233,11 @@ def ddm_device(img_seq, lags: Sequence[int], nx: int, ny: int, nt: int, window=N
                precision: str = "ff", gpu_id: int = 0, host_out: bool = False):
     """Run the structure function; returns the device result tensor (and the host copy if `host_out`).
 
-    Device-resident input (a CUDA tensor) is used in place; host input (numpy
-    or a CPU tensor) is uploaded in chunks overlapped with the spatial FFTs.
+    Device-resident input (a CUDA tensor) is used in place.  Page-locked host
+    input (a pinned CPU tensor whose rows are multiples of 16 bytes) is read in
+    place by the row pass, without a device copy of the stack; other host
+    input (numpy arrays, pageable tensors) is uploaded in chunks overlapped
+    with the spatial FFTs.
     """
     _require_torch()
     device = _device(gpu_id)
@@ -255,8 +262,20 @@ def ddm_device(img_seq, lags: Sequence[int], nx: int, ny: int, nt: int, window=N
         if hout is not None:
             hout.copy_(out, non_blocking=True)
     else:
-        staging = torch.empty(_host_nbytes(host), dtype=torch.uint8, device=device)
-        plan.run_from_host(host, staging, wdev, out, hout, stream)
+        # page-locked frames with 16-byte aligned rows are read in place: no device copy of the stack
+        in_place = (isinstance(host, torch.Tensor) and host.is_pinned() and host.data_ptr() % 16 == 0
+                    and (host.shape[-1] * host.element_size()) % 16 == 0)
+        done = False
+        if in_place:
+            try:
+                plan.run_from_host(host, None, wdev, out, hout, stream)
+                done = True
+            except _lib.FddmError as e:  # e.g. FDDM_B200_ZERO_COPY=0: nothing was queued, upload instead
+                if e.code != _lib.FDDM_ERR_INVALID:
+                    raise
+        if not done:
+            staging = torch.empty(_host_nbytes(host), dtype=torch.uint8, device=device)
+            plan.run_from_host(host, staging, wdev, out, hout, stream)
     if hout is not None:
         stream.synchronize()  # the host arrays must outlive the queued copies
         return out, hout

@@ -11,6 +11,7 @@
 
 namespace {
 thread_local std::string g_last_error;
+thread_local int g_last_input_path = 0;
 
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -35,7 +36,8 @@ int run(int mode, const void* img, int dtype, uint64_t length, uint64_t height, 
         double* out, void* work, size_t work_bytes, int precision, void* stream,
         const void* host_img = nullptr, double* host_out = nullptr) {
   g_last_error.clear();
-  if (!img || !out || (nlags && !lags) || !work) return fail(FDDM_ERR_INVALID, "null pointer argument");
+  // host frames read in place need no device frame buffer (the pipeline checks that they can be)
+  if ((!img && !host_img) || !out || (nlags && !lags) || !work) return fail(FDDM_ERR_INVALID, "null pointer argument");
   fddm::DdmRequest r;
   r.host_img = host_img;
   r.host_out = host_out;
@@ -74,6 +76,7 @@ std::map<int, StageEvents> g_events;  // per device
 }  // namespace
 
 void count_launches(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+void set_last_input_path(int path) { g_last_input_path = path; }
 
 namespace {
 std::mutex g_copy_mu;
@@ -190,6 +193,8 @@ int fddm_b200_stage_times(float* spatial_ms, float* temporal_ms) {
 }
 
 uint64_t fddm_b200_launch_count(void) { return fddm::g_launches.load(); }
+
+int fddm_b200_last_input_path(void) { return g_last_input_path; }
 
 int fddm_b200_ddm_from_host(int mode, const void* h_img_seq, int dtype, uint64_t length, uint64_t height,
                             uint64_t width, const uint32_t* lags, uint64_t nlags, uint64_t nx, uint64_t ny,

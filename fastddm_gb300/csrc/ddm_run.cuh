@@ -100,6 +100,37 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     err = "workspace too small: need " + std::to_string(L.total) + " bytes, got " + std::to_string(r.work_bytes);
     return 2;
   }
+  // Page-locked host frames (mapped into the device's address space under
+  // unified addressing; NVLink-C2C on Grace parts) are read in place by the row
+  // pass: no copy-engine upload, no staging.  Pageable frames are uploaded chunk
+  // by chunk on the copy stream: they may be views of memory-mapped files whose
+  // pages are not resident, which the kernels must not read directly.
+  // In-place reads also need the row pass's staged path (16-byte aligned rows,
+  // fetched with cp.async ahead of use): its per-pixel fallback would wait on
+  // every host read.  FDDM_B200_ZERO_COPY=0 forces the upload for page-locked
+  // frames too.
+  const size_t row_bytes = (size_t)r.W * dtype_bytes(r.dtype);
+  const size_t stage = (size_t)2 * L.pairs_per_block * row_bytes;
+  auto stageable = [&](const void* p) {
+    return row_bytes % 16 == 0 && (reinterpret_cast<uintptr_t>(p) % 16) == 0 && 2 * stage <= 64 * 1024;
+  };
+  const void* host_direct = nullptr;
+  if (r.host_img) {
+    const char* zc = std::getenv("FDDM_B200_ZERO_COPY");
+    cudaPointerAttributes pa{};
+    if (!(zc && zc[0] == '0') && cudaPointerGetAttributes(&pa, r.host_img) == cudaSuccess &&
+        pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr && stageable(pa.devicePointer))
+      host_direct = pa.devicePointer;
+    else
+      (void)cudaGetLastError();  // some runtimes report pageable memory as an error: clear it
+  }
+  set_last_input_path(r.host_img == nullptr ? 0 : host_direct ? 1 : 2);
+  if (r.host_img && !host_direct && r.img == nullptr) {
+    err = "the host frames cannot be read in place (pageable, not 16-byte aligned rows, or FDDM_B200_ZERO_COPY=0): "
+          "a device buffer for their upload is needed";
+    return 1;
+  }
+  const bool upload = r.host_img != nullptr && host_direct == nullptr;
   const int kind = tier_kind<S>::v;
   const int T = (int)r.T, H = (int)r.H, W = (int)r.W, nx = (int)r.nx, ny = (int)r.ny;
   const int nkx = nx / 2 + 1;
@@ -187,31 +218,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   if (evs) cudaEventRecord(evs->ev[0], st);
   int launches = r.window ? 1 : 0;
 
-  // Page-locked host frames (mapped into the device's address space under
-  // unified addressing; NVLink-C2C on Grace parts) are read in place by the row
-  // pass: no copy-engine upload, no staging.  Pageable frames are uploaded chunk
-  // by chunk on the copy stream: they may be views of memory-mapped files whose
-  // pages are not resident, which the kernels must not read directly.
-  // In-place reads also need the row pass's staged path (16-byte aligned rows,
-  // fetched with cp.async ahead of use): its per-pixel fallback would wait on
-  // every host read.  FDDM_B200_ZERO_COPY=0 forces the upload for page-locked
-  // frames too.
-  const size_t row_bytes = (size_t)W * dtype_bytes(r.dtype);
-  const size_t stage = (size_t)2 * L.pairs_per_block * row_bytes;
-  auto stageable = [&](const void* p) {
-    return row_bytes % 16 == 0 && (reinterpret_cast<uintptr_t>(p) % 16) == 0 && 2 * stage <= 64 * 1024;
-  };
-  const void* host_direct = nullptr;
-  if (r.host_img) {
-    const char* zc = std::getenv("FDDM_B200_ZERO_COPY");
-    cudaPointerAttributes pa{};
-    if (!(zc && zc[0] == '0') && cudaPointerGetAttributes(&pa, r.host_img) == cudaSuccess &&
-        pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr && stageable(pa.devicePointer))
-      host_direct = pa.devicePointer;
-    else
-      (void)cudaGetLastError();  // some runtimes report pageable memory as an error: clear it
-  }
-  const bool upload = r.host_img != nullptr && host_direct == nullptr;
+
 
   // stages 1-2 over frame chunks
   SpatialArgs sa{};

@@ -124,6 +124,7 @@ struct WorkLayout {
   int nt_fft;  // temporal transform length actually used (fft mode)
   int long_R0;  // fft mode: >0 selects the long-series kernel with this first radix
   int diff_staged;  // diff mode: 1 when the series is staged in shared memory
+  bool over_max_work = false;  // plan_layout failed only because DdmRequest::max_work is too small
 };
 
 // Upper bound on the temporal kernel's grid (sizes its per-CTA scratch).
@@ -148,6 +149,9 @@ int fail_with(int code, const std::string& msg);
 
 // Diagnostics: kernel launch counter and optional stage events.
 void count_launches(int n);
+// How the last call on this thread took its frames: 0 device memory, 1 host
+// memory read in place, 2 host memory uploaded (fddm_b200_last_input_path).
+void set_last_input_path(int path);
 struct StageEvents {
   bool enabled;
   cudaEvent_t ev[3];

@@ -18,8 +18,12 @@
 //     start at zero, but calls whose work overlaps on the GPU (two streams, or
 //     two host threads) race on the array and must be serialised by the caller;
 //   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current and caches it; make that
-//     first call before any stream capture begins.
+//     (cudaGetSymbolAddress) with that device current and caches it.  Under
+//     lazy module loading (the CUDA default) that lookup is also when the
+//     device reserves the 64 MiB, so a caller that reserves its device memory
+//     up front, or captures streams into graphs, makes one first call (any
+//     valid problem that fits) before doing so.  If the device has no room
+//     left at that point the call returns FDDM_ERR_NOMEM.
 #include <map>
 #include <mutex>
 #include <string>
@@ -45,7 +49,15 @@ int scratch_address(void** out) {
   auto it = g_addr.find(dev);
   if (it == g_addr.end()) {
     void* p = nullptr;
+    // under lazy module loading (the CUDA default) this first lookup loads the
+    // module that holds the array, which is when the device reserves its memory
     ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (ce == cudaErrorMemoryAllocation) {
+      (void)cudaGetLastError();
+      return fddm::fail_with(FDDM_ERR_NOMEM,
+                             "the device has no room for the 64 MiB static scratch of fddm_b200_ddm_fft_noalloc "
+                             "(reserved by the first call on a device)");
+    }
     if (ce != cudaSuccess || p == nullptr)
       return fddm::fail_with(FDDM_ERR_CUDA, std::string("cudaGetSymbolAddress of the static scratch failed: ") +
                                                 cudaGetErrorString(ce));
@@ -91,9 +103,9 @@ extern "C" int fddm_b200_ddm_fft_noalloc(const void* d_img_seq, int dtype, uint6
   std::string err;
   fddm::WorkLayout L;
   if (!fddm::plan_layout(r, L, err)) {
-    const bool too_big = err.find("workspace") != std::string::npos;
-    return fddm::fail_with(too_big ? FDDM_ERR_NOMEM : FDDM_ERR_UNSUPPORTED,
-                           too_big ? "the static scratch of fddm_b200_ddm_fft_noalloc is too small: " + err : err);
+    if (L.over_max_work)
+      return fddm::fail_with(FDDM_ERR_NOMEM, "the static scratch of fddm_b200_ddm_fft_noalloc is too small: " + err);
+    return fddm::fail_with(FDDM_ERR_UNSUPPORTED, err);
   }
   void* scratch = nullptr;
   const int rc0 = scratch_address(&scratch);

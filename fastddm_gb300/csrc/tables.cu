@@ -489,6 +489,7 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
     int c = (int)std::min<size_t>((size_t)L.chunk, room / std::max<size_t>(per_frame, 1));
     c = c / L.frames_per_block * L.frames_per_block;
     if (c < L.frames_per_block) {
+      L.over_max_work = true;
       err = "needs " + std::to_string(fixed + (size_t)L.frames_per_block * per_frame) +
             " bytes of workspace, more than the " + std::to_string(r.max_work) + " available";
       return false;

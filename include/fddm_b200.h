@@ -111,7 +111,9 @@ int fddm_b200_ddm_diff(const void* d_img_seq, int dtype, uint64_t length, uint64
    take host arrays: src/cpp/ddm.h:38-61).  Page-locked frames (mapped into
    the device's address space under unified addressing) are read in place by
    the spatial kernels, over NVLink-C2C on Grace parts, and d_frames is not
-   touched.  Pageable frames (or any, with FDDM_B200_ZERO_COPY=0 in the
+   touched (it may be NULL; that needs rows of a multiple of 16 bytes starting
+   on 16-byte boundaries, else the call fails with FDDM_ERR_INVALID before any
+   work is queued).  Pageable frames (or any, with FDDM_B200_ZERO_COPY=0 in the
    environment) are copied chunk by chunk from h_img_seq into the caller's
    device buffer
    d_frames (length*height*width elements) on a library copy stream; each
@@ -187,8 +189,12 @@ int fddm_b200_azimuthal_average(const double* d_data, uint64_t nrows, uint64_t n
    holds until the process exits; a problem needing more is rejected with
    FDDM_ERR_NOMEM.  All calls share that array, so calls that overlap on the GPU
    race and must be serialised by the caller.  The first call on a device looks
-   up the array's device address with that device current; make it before any
-   stream capture.  Arguments and result as fddm_b200_ddm_fft. */
+   up the array's device address with that device current, and under CUDA's
+   default lazy module loading that is also when the device reserves the
+   64 MiB: make one first call (any valid problem that fits) before reserving
+   the rest of device memory and before any stream capture.  Without room for
+   the array at that point the call returns FDDM_ERR_NOMEM.  Arguments and
+   result as fddm_b200_ddm_fft. */
 int fddm_b200_ddm_fft_noalloc(const void* d_img_seq, int dtype, uint64_t length, uint64_t height, uint64_t width,
                               const uint32_t* lags, uint64_t nlags, uint64_t nx, uint64_t ny, uint64_t nt,
                               const double* d_window, double* d_out, int precision, void* stream);
@@ -254,10 +260,15 @@ int fddm_b200_tiff_read(const char* path, const uint64_t* pages, uint64_t npages
    and the temporal stage; fddm_b200_stage_times waits for the last call's
    events and returns the two durations in milliseconds.
    fddm_b200_launch_count returns the number of kernels this library has
-   launched in the process so far. */
+   launched in the process so far.
+   fddm_b200_last_input_path tells how the last structure-function call on
+   the calling thread took its frames: 0 from device memory, 1 from host
+   memory read in place by the row pass, 2 from host memory uploaded to the
+   device buffer. */
 int fddm_b200_set_stage_timing(int enable);
 int fddm_b200_stage_times(float* spatial_ms, float* temporal_ms);
 uint64_t fddm_b200_launch_count(void);
+int fddm_b200_last_input_path(void);
 
 #ifdef __cplusplus
 }

@@ -148,6 +148,53 @@ def ddm_exact(img_seq: np.ndarray, lags: Iterable[int], nx: int, ny: int,
     return shift_y(out.reshape(len(lags) + 2, ny, nx // 2 + 1)).astype(np.float64)
 
 
+def sampled_exact(img_seq: np.ndarray, lags: Iterable[int], nx: int, ny: int, cols: Sequence[int],
+                  window: Optional[np.ndarray] = None, threads: int = 8) -> np.ndarray:
+    """D, PS and VAR at the kx columns `cols` (every ky), without cancellation, for large stacks.
+
+    The spectrum of the sampled columns comes from direct FP64 DFTs of every
+    frame (rows against exp(-2 pi i x kx / nx), then columns against
+    exp(-2 pi i y ky / ny), scaled by 1/sqrt(nx ny) as ddm.cc:319-323 does);
+    D(lag) by direct differences (src/cpp/ddm.cc:118-146), PS = <|F|^2>_t and
+    VAR = <|F - <F>_t|^2>_t.  Returns (L + 2, ny, len(cols)), y-fftshifted like
+    the full result's columns `cols`.  Its own error is ~1e-16 sqrt(PS / D).
+    """
+    from concurrent.futures import ThreadPoolExecutor
+
+    lags = [int(l) for l in lags]
+    T, H, W = img_seq.shape
+    C = len(cols)
+    ex = np.exp(-2j * np.pi * np.outer(np.arange(W), np.asarray(cols)) / nx)
+    exr = np.ascontiguousarray(np.concatenate([ex.real, ex.imag], axis=1))  # (W, 2C)
+    ey = np.exp(-2j * np.pi * np.outer(np.arange(ny), np.arange(H)) / ny)   # (ny, H), natural ky order
+    win = None if window is None or np.size(window) == 0 else np.asarray(window, dtype=np.float64)
+    F = np.empty((T, ny, C), dtype=np.complex128)
+    for t0 in range(0, T, 16):
+        blk = np.asarray(img_seq[t0:t0 + 16]).astype(np.float64)
+        if win is not None:
+            blk *= win
+        a = blk @ exr
+        F[t0:t0 + 16] = np.einsum("yh,thc->tyc", ey, a[..., :C] + 1j * a[..., C:], optimize=True)
+    F /= math.sqrt(float(nx * ny))
+    Fq = F.reshape(T, ny * C)
+
+    def chunk(c0):
+        f = Fq[:, c0:c0 + 256]
+        o = np.empty((len(lags) + 2, f.shape[1]))
+        for i, lag in enumerate(lags):
+            d = f[lag:] - f[: T - lag]
+            o[i] = (d.real * d.real + d.imag * d.imag).sum(axis=0) / float(T - lag)
+        o[-2] = (f.real * f.real + f.imag * f.imag).sum(axis=0) / float(T)
+        g = f - f.mean(axis=0)
+        o[-1] = (g.real * g.real + g.imag * g.imag).sum(axis=0) / float(T)
+        return o
+
+    with ThreadPoolExecutor(max_workers=threads) as ex_:
+        parts = list(ex_.map(chunk, range(0, ny * C, 256)))
+    out = np.concatenate(parts, axis=1).reshape(len(lags) + 2, ny, C)
+    return np.fft.fftshift(out, axes=1)
+
+
 # ---------------------------------------------------------------------------
 # front door pieces: src/python/_ddm.py:128-198, _fftopt.py:29-150
 # ---------------------------------------------------------------------------

@@ -18,6 +18,12 @@ def golden():
     return dict(np.load(ROOT / "tests" / "golden" / "golden.npz"))
 
 
+@pytest.fixture(scope="session")
+def golden_confocal():
+    """The reference test's own fixture at full size: 20 confocal frames of 256 x 256, lags 1..9."""
+    return dict(np.load(ROOT / "tests" / "golden" / "golden_confocal.npz"))
+
+
 def gpu_ready() -> bool:
     try:
         import torch

@@ -7,6 +7,10 @@ tree, and stores its outputs together with the inputs.  The reference's
 ``tests/test_ddm.py`` checks that this core agrees with the ``cpp`` core
 (``np.isclose``); the compiled cores themselves are not built here.
 
+It writes ``golden.npz`` (small cases and helper tables) and
+``golden_confocal.npz`` (the reference test's 20 confocal frames of 256 x 256
+at full size, lags 1..9, fft and diff mode).
+
 Usage (needs the reference checkout; the fixtures it writes are committed):
 
     python tests/golden/make_golden.py /path/to/fastddm-reference
@@ -140,6 +144,17 @@ def main(root: Path) -> None:
 
     np.savez_compressed(HERE / "golden.npz", **g)
     print("wrote", HERE / "golden.npz", sum(np.asarray(v).nbytes for v in g.values()), "bytes raw")
+
+    # case C: the reference test fixture at its full size, uncropped: confocal
+    # frames 0..19 of 256 x 256, lags 1..9 (tests/test_ddm.py:14-16), both modes
+    full = np.stack([read_tiff_u8(p) for p in files])
+    c = {"C_imgs": full, "C_lags": lags}
+    for mode in ("fft", "diff"):
+        r = ddm(full, lags, core="py", mode=mode)
+        c[f"C_{mode}"] = r._data
+    c["C_kx"], c["C_ky"] = r.kx, r.ky
+    np.savez_compressed(HERE / "golden_confocal.npz", **c)
+    print("wrote", HERE / "golden_confocal.npz", sum(np.asarray(v).nbytes for v in c.values()), "bytes raw")
 
 
 if __name__ == "__main__":

@@ -321,19 +321,32 @@ def test_backend_function_contract(fddm):
 
 
 @pytest.mark.parametrize("mode", ["fft", "diff"])
-def test_page_locked_frames_read_in_place_or_uploaded(fddm, monkeypatch, mode):
-    """Page-locked host frames are read by the row pass in place (no copy-engine upload);
-    FDDM_B200_ZERO_COPY=0 uploads them chunk by chunk instead: identical results."""
+def test_page_locked_frames_read_in_place_or_uploaded(fddm, built_lib, monkeypatch, mode):
+    """Page-locked host frames are read by the row pass in place (no copy-engine upload, no device
+    copy of the stack); FDDM_B200_ZERO_COPY=0 uploads them chunk by chunk instead: identical results.
+    Rows that are not a multiple of 16 bytes cannot be read in place and are uploaded."""
     import torch
 
     imgs = _poisson_stack((40, 72, 64), "uint8", seed=21, level=30.0)
     lags = [1, 2, 5, 13, 39]
     pinned = torch.from_numpy(imgs).pin_memory()
     direct = fddm.ddm(pinned, lags, mode=mode)._data
+    assert built_lib.fddm_b200_last_input_path() == 1
     monkeypatch.setenv("FDDM_B200_ZERO_COPY", "0")
     uploaded = fddm.ddm(pinned, lags, mode=mode)._data
+    assert built_lib.fddm_b200_last_input_path() == 2
+    monkeypatch.delenv("FDDM_B200_ZERO_COPY")
     np.testing.assert_array_equal(direct, uploaded)
     _check(direct, imgs, lags, mode, "ff", label="page-locked in place")
+    # 60-byte rows: the in-place read is refused before any work, the frames are uploaded
+    odd = torch.from_numpy(np.ascontiguousarray(imgs[:, :, :60])).pin_memory()
+    r = fddm.ddm(odd, lags, mode=mode)._data
+    assert built_lib.fddm_b200_last_input_path() == 2
+    np.testing.assert_array_equal(r, fddm.ddm(np.ascontiguousarray(imgs[:, :, :60]), lags, mode=mode)._data)
+    fddm.ddm(imgs, lags, mode=mode)
+    assert built_lib.fddm_b200_last_input_path() == 2  # pageable numpy: uploaded
+    fddm.ddm(pinned.cuda(), lags, mode=mode)
+    assert built_lib.fddm_b200_last_input_path() == 0  # device frames
 
 
 @pytest.mark.parametrize("mode", ["fft", "diff"])

@@ -35,6 +35,31 @@ def test_oracle_matches_reference_core(golden, mode, case, winkey, outkey):
     assert np.isclose(out, ref).all()  # the reference test's own criterion
 
 
+@pytest.mark.parametrize("mode", ["fft", "diff"])
+def test_oracle_matches_reference_core_full_fixture(golden_confocal, mode):
+    """The reference test's fixture uncropped (tests/test_ddm.py:14-16: 20 confocal frames of 256 x 256, lags 1..9)."""
+    g = golden_confocal
+    imgs, lags = g["C_imgs"], g["C_lags"]
+    nx, ny, nt = _sizes(imgs, mode)
+    out = oracle.ddm_fft(imgs, lags, nx, ny, nt) if mode == "fft" else oracle.ddm_diff(imgs, lags, nx, ny)
+    ref = g[f"C_{mode}"]
+    assert out.shape == ref.shape == (11, 256, 129)
+    assert oracle.rel_err(out, ref) < ORACLE_RTOL
+    assert np.isclose(out, ref).all()
+    kx, ky = oracle.axes(nx, ny)
+    np.testing.assert_array_equal(kx, g["C_kx"])
+    np.testing.assert_array_equal(ky, g["C_ky"])
+
+
+def test_sampled_exact_matches_full_exact(golden):
+    """The sampled direct-DFT yardstick (used at full sizes) equals the extended-precision one on its columns."""
+    imgs, lags, w = golden["B_imgs"], golden["B_lags"], golden["B_window"]
+    nx, ny, _ = _sizes(imgs, "fft")
+    cols = [0, 1, 4, nx // 2]
+    full = oracle.ddm_exact(imgs, lags, nx, ny, w)
+    assert oracle.rel_err(oracle.sampled_exact(imgs, lags, nx, ny, cols, w), full[:, :, cols]) < 1e-11
+
+
 def test_oracle_fft_vs_diff_agree(golden):
     imgs, lags = golden["A_imgs"], golden["A_lags"]
     nx, ny, nt = _sizes(imgs, "fft")

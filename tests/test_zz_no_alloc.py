@@ -33,7 +33,10 @@ def _frames(shape, seed):
     return np.stack(out).astype(np.uint16)
 
 
-def _run_pair(lib, torch, imgs, lags, window):
+PREC = {"ff": 0, "f64": 1, "f32": 2}
+
+
+def _run_pair(lib, torch, imgs, lags, window, precision="ff", calls=2):
     from fastddm_gb300 import _lib
     from fastddm_gb300._fftopt import next_fast_len
 
@@ -50,19 +53,20 @@ def _run_pair(lib, torch, imgs, lags, window):
     stream = torch.cuda.current_stream(dev).cuda_stream
 
     size = ctypes.c_size_t()
-    _lib.check(lib.fddm_b200_workspace_size(0, 0, T, H, W, len(lags_c), nx, ny, nt, int(win is not None),
+    prec = PREC[precision]
+    _lib.check(lib.fddm_b200_workspace_size(0, prec, T, H, W, len(lags_c), nx, ny, nt, int(win is not None),
                                             ctypes.byref(size)))
     work = torch.empty(size.value, dtype=torch.uint8, device=dev)
     ref = torch.empty(shape, dtype=torch.float64, device=dev)
     _lib.check(lib.fddm_b200_ddm_fft(frames.data_ptr(), code, T, H, W, lp, len(lags_c), nx, ny, nt, wptr,
-                                     ref.data_ptr(), work.data_ptr(), size.value, 0, stream))
+                                     ref.data_ptr(), work.data_ptr(), size.value, prec, stream))
     outs = []
-    for _ in range(2):  # two calls in a row share the static scratch
+    for _ in range(calls):  # calls in a row share the static scratch
         out = torch.full(shape, float("nan"), dtype=torch.float64, device=dev)
         _lib.check(lib.fddm_b200_ddm_fft_noalloc(frames.data_ptr(), code, T, H, W, lp, len(lags_c), nx, ny, nt,
-                                                 wptr, out.data_ptr(), 0, stream))
+                                                 wptr, out.data_ptr(), prec, stream))
         outs.append(out.cpu().numpy())
-    return ref.cpu().numpy(), outs
+    return ref.cpu().numpy(), outs, size.value
 
 
 @pytest.mark.parametrize("shape,lags,windowed", [
@@ -75,10 +79,30 @@ def test_noalloc_matches_workspace_entry_point(built_lib, shape, lags, windowed)
 
     imgs = _frames(shape, seed=shape[0])
     window = blackman_harris(shape) if windowed else None
-    ref, outs = _run_pair(built_lib, torch, imgs, lags, window)
+    ref, outs, _ = _run_pair(built_lib, torch, imgs, lags, window)
     for out in outs:
         assert np.all(np.isfinite(out))
         np.testing.assert_allclose(out, ref, rtol=RTOL, atol=0.0)
+
+
+def test_noalloc_shrinks_its_frame_chunk_and_alternates_problems(built_lib):
+    """A problem whose workspace (at the full frame chunk) exceeds the 64 MiB array but fits once the
+    frame chunk shrinks, alternated with another shape and tier: each call starts from the array the
+    previous, different problem left behind, and must still equal its workspace twin."""
+    torch = pytest.importorskip("torch")
+
+    small = _frames((40, 48, 64), seed=40)
+    big = _frames((520, 128, 128), seed=520)  # FP32 tier: ~74 MiB of workspace at the full chunk
+    for imgs, lags, precision in ((small, [1, 2, 3, 5, 8, 13, 21, 39], "ff"),
+                                  (big, list(range(1, 520)), "f32"),
+                                  (small, [1, 2, 3, 5, 8, 13, 21, 39], "ff"),
+                                  (big, list(range(1, 520)), "f32")):
+        ref, outs, need = _run_pair(built_lib, torch, imgs, lags, None, precision, calls=1)
+        if imgs is big:
+            assert need > 64 << 20  # only the shrunken frame chunk fits the static scratch
+        for out in outs:
+            assert np.all(np.isfinite(out))
+            np.testing.assert_allclose(out, ref, rtol=RTOL, atol=0.0)
 
 
 def test_noalloc_rejects_problems_beyond_its_scratch(built_lib):
