@@ -494,7 +494,36 @@ __device__ __forceinline__ void pair_power(cx<S>* __restrict__ buf, int M1, int 
   }
 }
 
-template <class S, class A, bool P2>
+// Plans whose first radix is 2 (F2 path of the temporal kernel): the length-N
+// forward transform's last pass (radix R, stride 1), the pairing of P(2m) at
+// position p with P(2m+1) at N/2 + p, and the half plan's first inverse pass
+// (the same radix R, stride 1, no twiddles) run as one step: the thread that
+// transforms block b of the lower half and block b of the upper half holds
+// both powers of every position of block b and transforms them on in
+// registers, writing only the lower half.
+template <class S, int R>
+__device__ __forceinline__ void last_pass_pair_first_inverse(cx<S>* __restrict__ buf, int N2, int tid, int nthr) {
+  for (int b = tid; b < N2 / R; b += nthr) {
+    cx<S> v[R], u[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) v[i] = buf[swz<S>(b * R + i)];
+    dft<S, R, false>(v);
+#pragma unroll
+    for (int i = 0; i < R; ++i) u[i] = buf[swz<S>(N2 + b * R + i)];
+    dft<S, R, false>(u);
+#pragma unroll
+    for (int i = 0; i < R; ++i) v[i] = {sc<S>::sqsum(v[i].r, v[i].i), sc<S>::neg(sc<S>::sqsum(u[i].r, u[i].i))};
+    dft<S, R, true>(v);
+#pragma unroll
+    for (int i = 0; i < R; ++i) buf[swz<S>(b * R + i)] = v[i];
+  }
+}
+
+// F2: first radix 2, N/2 a multiple of the swizzle group and all radices 2, 4
+// or 8 (host: fused_radix2_ok).  The padded radix-2 first pass is folded into
+// the pass over the series (G at t and G w_N^t at N/2 + t), and the last
+// forward pass, the pairing and the first inverse pass run as one step.
+template <class S, class A, bool P2, bool F2 = false>
 __device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int T = a.T, N = a.nt, N2 = a.nt / 2, nl = a.nlags;
@@ -518,6 +547,7 @@ __device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
   const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
   const cx<S>* F = reinterpret_cast<const cx<S>*>(a.spec);
   const cx<S>* tw = reinterpret_cast<const cx<S>*>(a.twt);
+  const cx<S>* p0tw = reinterpret_cast<const cx<S>*>(a.pt.ptw[0]);  // w_N^t, the radix-2 first pass's table
   const A invT = sc<A>::cst(a.invT_h, a.invT_l, a.invT_d);
   const A invN = sc<A>::cst(a.invnt_h, a.invnt_l, a.invnt_d);
   const int chunk = (T + nthr - 1) / nthr;
@@ -559,6 +589,7 @@ __device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
     mi = shfl_idx(warp_sum(mi), 0);
     const A inv_ref = sc<A>::from_double(1.0 / nref);
     const S msr = cvt<S, A>::to_fft(sc<A>::mul(mr, inv_ref)), msi = cvt<S, A>::to_fft(sc<A>::mul(mi, inv_ref));
+    if (F2) __syncthreads();  // the upper half written below overlays the series every warp just sampled
 
     // G = F - m into buf[0, T), over a contiguous chunk per thread: sums of G
     // and of |G|^2 for the statistics and the prefix sums
@@ -569,6 +600,8 @@ __device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
       g.r = sc<S>::sub(g.r, msr);
       g.i = sc<S>::sub(g.i, msi);
       buf[swz<S>(t)] = g;
+      // the padded radix-2 first pass: x_t and x_t w_N^t (N/2 + t is the slot of ser[t] itself)
+      if (F2) buf[swz<S>(N2 + t)] = twmul<S>::mul(g, p0tw[t]);
       if (t < kDirect) head[t] = g;
       if (t >= tail0) tail[t - tail0] = g;
       const A gr = cvt<S, A>::to_acc(g.r), gi = cvt<S, A>::to_acc(g.i);
@@ -576,18 +609,8 @@ __device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
       sgr = sc<A>::add(sgr, gr);
       sgi = sc<A>::add(sgi, gi);
     }
-    A total;  // also left in scratch[32] until the next mode's scan
+    A total;  // also left in scratch[32] (the sums of G in [33], [34]) until the next mode's scan
     A pre = block_scan_sum2<A>(run, total, sgr, sgi, scratch);
-    if (tid == 0) {
-      // <G> (rounding-size), VAR = <|G|^2> - |<G>|^2, PS = <|G|^2> + 2 Re(conj(m) <G>) + |m|^2
-      const A gmr = sc<A>::mul(sgr, invT), gmi = sc<A>::mul(sgi, invT);
-      const A g2 = sc<A>::mul(total, invT);
-      const A mr = cvt<S, A>::to_acc(msr), mi = cvt<S, A>::to_acc(msi);
-      const A cross = sc<A>::add(sc<A>::mul(mr, gmr), sc<A>::mul(mi, gmi));
-      const A ps = sc<A>::add(sc<A>::add(g2, sc<A>::add(cross, cross)), sc<A>::sqsum(mr, mi));
-      a.out[(size_t)nl * a.Q + q] = sc<A>::to_double(ps);
-      a.out[(size_t)(nl + 1) * a.Q + q] = sc<A>::to_double(sc<A>::sub(g2, sc<A>::sqsum(gmr, gmi)));
-    }
     // prefix sums pfx[t + 1] = sum_{s <= t} |G(s)|^2, stored at the slots the lags need
     for (int t = t_beg; t < t_end; ++t) {
       const cx<S> g = buf[swz<S>(t)];
@@ -597,19 +620,55 @@ __device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
       if (sb >= 0) need[nl + sb] = pre;
     }
     if (tid == 0 && slotB[0] >= 0) need[nl + slotB[0]] = sc<A>::zero();
+    if (F2) {
+      for (int t = T + tid; t < N2; t += nthr) {
+        buf[swz<S>(t)] = czero<S>();
+        buf[swz<S>(N2 + t)] = czero<S>();
+      }
+    }
     __syncthreads();
 
-    fft_forward_padded<S, P2>(buf, a.pt, T, tw, tid, nthr);
-    if (R0 == 8) pair_power<S, 8>(buf, M1, tid, nthr);
-    else if (R0 == 4) pair_power<S, 4>(buf, M1, tid, nthr);
-    else pair_power<S, 2>(buf, M1, tid, nthr);
-    __syncthreads();
-    // buf above the half-length transform is free: start loading the next mode
-    if (q + gridDim.x < a.q_end) prefetch_series<S>(ser, F + (q + gridDim.x) * a.Tpad, T, tid, nthr);
-    // the length-N table serves the half-length passes: w_M^k = tw[k N / M]
-    fft_inverse<S, P2>(buf, 1, N2, a.pt2, tw, tid, nthr, N);
+    if (F2) {
+      const int np = a.pt.npass;
+      for (int s = 1; s < np - 1; ++s) {
+        fft_pass_dispatch<S, false, true>(buf, 1, N, a.pt, s, tw, N, tid, nthr);
+        __syncthreads();
+      }
+      const int R = a.pt.radix[np - 1];
+      if (R == 8) last_pass_pair_first_inverse<S, 8>(buf, N2, tid, nthr);
+      else if (R == 4) last_pass_pair_first_inverse<S, 4>(buf, N2, tid, nthr);
+      else last_pass_pair_first_inverse<S, 2>(buf, N2, tid, nthr);
+      __syncthreads();
+      if (q + gridDim.x < a.q_end) prefetch_series<S>(ser, F + (q + gridDim.x) * a.Tpad, T, tid, nthr);
+      // remaining inverse passes of the half plan (its last pass ran above)
+      for (int s = a.pt2.npass - 2; s >= 0; --s) {
+        fft_pass_dispatch<S, true, true>(buf, 1, N2, a.pt2, s, tw, N, tid, nthr);
+        __syncthreads();
+      }
+    } else {
+      fft_forward_padded<S, P2>(buf, a.pt, T, tw, tid, nthr);
+      if (R0 == 8) pair_power<S, 8>(buf, M1, tid, nthr);
+      else if (R0 == 4) pair_power<S, 4>(buf, M1, tid, nthr);
+      else pair_power<S, 2>(buf, M1, tid, nthr);
+      __syncthreads();
+      // buf above the half-length transform is free: start loading the next mode
+      if (q + gridDim.x < a.q_end) prefetch_series<S>(ser, F + (q + gridDim.x) * a.Tpad, T, tid, nthr);
+      // the length-N table serves the half-length passes: w_M^k = tw[k N / M]
+      fft_inverse<S, P2>(buf, 1, N2, a.pt2, tw, tid, nthr, N);
+    }
 
     total = scratch[32];
+    // PS and VAR, by the thread after the last lag (off the barrier-bound path of the transform):
+    // <G> (rounding-size), VAR = <|G|^2> - |<G>|^2, PS = <|G|^2> + 2 Re(conj(m) <G>) + |m|^2
+    if (tid == (nl < nthr ? nl : nthr - 1)) {
+      const A gmr = sc<A>::mul(scratch[33], invT), gmi = sc<A>::mul(scratch[34], invT);
+      const A g2 = sc<A>::mul(total, invT);
+      const A mr = cvt<S, A>::to_acc(msr), mi = cvt<S, A>::to_acc(msi);
+      const A cross = sc<A>::add(sc<A>::mul(mr, gmr), sc<A>::mul(mi, gmi));
+      const A ps = sc<A>::add(sc<A>::add(g2, sc<A>::add(cross, cross)), sc<A>::sqsum(mr, mi));
+      a.out[(size_t)nl * a.Q + q] = sc<A>::to_double(ps);
+      a.out[(size_t)(nl + 1) * a.Q + q] = sc<A>::to_double(sc<A>::sub(g2, sc<A>::sqsum(gmr, gmi)));
+    }
     for (int l = tid; l < nl; l += nthr) {
       const int tau = a.need_in_smem ? FDDM_LAG_TAU[l] : a.lags[l];
       if (T - tau <= kDirect) continue;
@@ -650,14 +709,14 @@ __device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
 #undef FDDM_LAG_TAU
 }
 
-template <class S, class A, bool P2>
+template <class S, class A, bool P2, bool F2 = false>
 __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
-  tfft_body<S, A, P2>(a);
+  tfft_body<S, A, P2, F2>(a);
 }
 // FP32 transforms: two 512-thread CTAs per SM (their shared memory allows it)
-template <class S, class A, bool P2>
+template <class S, class A, bool P2, bool F2 = false>
 __global__ void __launch_bounds__(512, 2) k_tfft_x2(TemporalArgs a) {
-  tfft_body<S, A, P2>(a);
+  tfft_body<S, A, P2, F2>(a);
 }
 
 // ---------------------------------------------------------------------------
@@ -941,7 +1000,10 @@ __global__ void __launch_bounds__(512) k_tdiff(TemporalArgs a) {
     A v[3] = {sc<A>::zero(), sc<A>::zero(), sc<A>::zero()};
     for (int t = tid; t < T; t += nthr) {
       const cx<S> f = buf[t];
-      const A fr = cvt<S, A>::to_acc(f.r), fi = cvt<S, A>::to_acc(f.i);
+      // the spectrum's float-float pairs are not renormalised (butterfly sums):
+      // after cancellation the low word can be a sizeable fraction of the high
+      // word, whose square ff_sqsum would drop
+      const A fr = canon(cvt<S, A>::to_acc(f.r)), fi = canon(cvt<S, A>::to_acc(f.i));
       v[0] = sc<A>::add(v[0], fr);
       v[1] = sc<A>::add(v[1], fi);
       v[2] = sc<A>::add(v[2], sc<A>::sqsum(fr, fi));

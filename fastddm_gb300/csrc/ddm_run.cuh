@@ -51,16 +51,34 @@ inline bool plan_is_p2(const FftPlan& p) {
 }
 
 // Temporal kernel of a tier: FP32 transforms run two CTAs per SM.
-template <class S, class A, bool P2> constexpr auto tfft_kernel() {
-  if constexpr (sizeof(S) == 4) return &k_tfft_x2<S, A, P2>;
-  else return &k_tfft<S, A, P2>;
+template <class S, class A, bool P2, bool F2 = false> constexpr auto tfft_kernel() {
+  if constexpr (sizeof(S) == 4) return &k_tfft_x2<S, A, P2, F2>;
+  else return &k_tfft<S, A, P2, F2>;
+}
+
+// The temporal kernel's fused radix-2 path (F2 in tfft_body): first radix 2,
+// every radix 2, 4 or 8, at least two passes, and N/2 a multiple of the square
+// of the swizzle group, so that slot N/2 + t of the transform buffer is the
+// slot of element t of the series prefetched at N/2.
+template <class S> inline bool fused_radix2_ok(const FftPlan& p) {
+  const int G = swz_group<S>::G;
+  return plan_is_p2(p) && p.npass >= 2 && p.radix[0] == 2 && (p.n / 2) % (G * G) == 0;
+}
+
+// CTA sizes of the spatial passes; FDDM_B200_ROWS_THREADS / FDDM_B200_COLS_THREADS
+// (128, 256 or 512) override them (tuning).
+inline int spatial_threads(const char* env, int dflt) {
+  const char* v = std::getenv(env);
+  const int x = v ? std::atoi(v) : 0;
+  return (x == 128 || x == 256 || (x == 512 && dflt == 512)) ? x : dflt;
 }
 
 template <class S, class IN, bool P2>
 cudaError_t launch_rows(const SpatialArgs& a, int items, size_t smem, cudaStream_t st) {
   cudaError_t e = allow_smem(k_rows<S, IN, P2>, smem);
   if (e != cudaSuccess) return e;
-  k_rows<S, IN, P2><<<persistent_grid(k_rows<S, IN, P2>, 256, smem, items), 256, smem, st>>>(a);
+  const int nt = spatial_threads("FDDM_B200_ROWS_THREADS", 256);
+  k_rows<S, IN, P2><<<persistent_grid(k_rows<S, IN, P2>, nt, smem, items), nt, smem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -296,8 +314,9 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     }
     const int col_items = ((nkx + L.cols_per_block - 1) / L.cols_per_block) *
                           ((sa.tc + L.frames_per_block - 1) / L.frames_per_block);
-    if (p2y) k_cols<S, true><<<persistent_grid(k_cols<S, true>, 512, smem_cols, col_items), 512, smem_cols, st>>>(sa);
-    else k_cols<S, false><<<persistent_grid(k_cols<S, false>, 512, smem_cols, col_items), 512, smem_cols, st>>>(sa);
+    const int ct = spatial_threads("FDDM_B200_COLS_THREADS", 512);
+    if (p2y) k_cols<S, true><<<persistent_grid(k_cols<S, true>, ct, smem_cols, col_items), ct, smem_cols, st>>>(sa);
+    else k_cols<S, false><<<persistent_grid(k_cols<S, false>, ct, smem_cols, col_items), ct, smem_cols, st>>>(sa);
     if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
     launches += 2;
   }
@@ -337,25 +356,58 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
       const size_t with_need = temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), true);
       ta.need_in_smem = with_need <= kSmemLimit ? 1 : 0;
       smem_t = temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), ta.need_in_smem != 0);
-      threads = temporal_threads(N);
+      threads = 0;  // chosen below by occupancy
     }
   } else if (!L.diff_staged) {
     smem_t = 96 * sizeof(A);
   }
   const bool p2t = r.mode == MODE_FFT && !long_fft && plan_is_p2(ta.pt) && plan_is_p2(ta.pt2);
+  // FDDM_B200_TEMPORAL_FUSED=0 keeps the separate passes (comparison runs)
+  const char* fz = std::getenv("FDDM_B200_TEMPORAL_FUSED");
+  const bool f2t = p2t && fused_radix2_ok<S>(ta.pt) && !(fz && fz[0] == '0');
   ta.lags = d_lags; ta.rcp = d_rcp; ta.out = r.out;
   split_ff(1.0 / (double)T, ta.invT_h, ta.invT_l); ta.invT_d = 1.0 / (double)T;
   int dev = 0, nsm = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  // CTA size of the shared-memory temporal kernels: the candidate that keeps the
+  // most warps resident per SM, the smallest such CTA on ties.  Each CTA works
+  // on its own mode, so several smaller CTAs per SM keep issuing while one of
+  // them waits at a barrier (measured on 512^2 stacks, 200 lags: 1.18x at
+  // T = 2000, 1.5x at T = 1000, 2.2x at T = 500 against one radix-8 butterfly
+  // per thread).  FDDM_B200_TEMPORAL_THREADS=128|256|512 overrides the choice.
+  auto pick_threads = [&](auto kernel) {
+    if (const char* tt = std::getenv("FDDM_B200_TEMPORAL_THREADS")) {
+      const int v = std::atoi(tt);
+      if (v == 128 || v == 256 || v == 512) return v;
+    }
+    int best = 512, best_warps = 0;
+    for (int t : {512, 256, 128}) {
+      int o = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kernel, t, smem_t) != cudaSuccess) {
+        (void)cudaGetLastError();
+        continue;
+      }
+      // the long-series kernel's per-CTA scratch holds kMaxLongCtas CTAs
+      if (long_fft) o = std::min(o, std::max(1, kMaxLongCtas / std::max(nsm, 1)));
+      if (o * t / 32 >= best_warps && o > 0) {
+        best_warps = o * t / 32;
+        best = t;
+      }
+    }
+    return best;
+  };
   auto prepare = [&](auto kernel) -> bool {
     if ((ce = allow_smem(kernel, smem_t)) != cudaSuccess) { err = cudaGetErrorString(ce); return false; }
+    threads = pick_threads(kernel);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem_t);
     return true;
   };
   bool prepared;
   if (long_fft) prepared = prepare(k_tfft_long<S, A>);
-  else if (r.mode == MODE_FFT) prepared = p2t ? prepare(tfft_kernel<S, A, true>()) : prepare(tfft_kernel<S, A, false>());
+  else if (r.mode == MODE_FFT)
+    prepared = f2t ? prepare(tfft_kernel<S, A, true, true>())
+                   : p2t ? prepare(tfft_kernel<S, A, true>()) : prepare(tfft_kernel<S, A, false>());
   else if (L.diff_staged) prepared = prepare(k_tdiff<S, A, true>);
   else prepared = prepare(k_tdiff<S, A, false>);
   if (!prepared) return 3;
@@ -373,6 +425,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     const unsigned grid = (unsigned)std::min<size_t>(ta.q_end - ta.q_begin, max_grid);
     if (grid == 0) continue;
     if (long_fft) k_tfft_long<S, A><<<grid, threads, smem_t, st>>>(ta);
+    else if (r.mode == MODE_FFT && f2t) tfft_kernel<S, A, true, true>()<<<grid, threads, smem_t, st>>>(ta);
     else if (r.mode == MODE_FFT && p2t) tfft_kernel<S, A, true>()<<<grid, threads, smem_t, st>>>(ta);
     else if (r.mode == MODE_FFT) tfft_kernel<S, A, false>()<<<grid, threads, smem_t, st>>>(ta);
     else if (L.diff_staged) k_tdiff<S, A, true><<<grid, threads, smem_t, st>>>(ta);

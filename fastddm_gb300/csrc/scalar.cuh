@@ -77,6 +77,10 @@ __device__ __forceinline__ ff ff_sqsum(ff a, ff b) {
   return fast_two_sum(s.h, t);
 }
 
+// Canonical form of a pair whose low word may be as large as the high word
+// (butterfly sums without renormalisation leave such pairs after cancellation).
+__device__ __forceinline__ ff ff_canon(ff a) { return two_sum(a.h, a.l); }
+
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.h + (double)a.l; }
 __host__ __device__ __forceinline__ ff ff_from_float(float a) { return {a, 0.0f}; }
 // FP64 -> ff (round-to-nearest hi, exact remainder rounded to float)
@@ -137,6 +141,11 @@ template <> struct sc<double> {
   static __device__ __forceinline__ double cst(float h, float l, double d) { return d; }
   static __device__ __forceinline__ double mul_p2(double a, float p2) { return a * (double)p2; }
 };
+
+// Canonical form before products that drop the low word's square (ff_sqsum):
+// identity for native types.
+template <class A> __device__ __forceinline__ A canon(A a) { return a; }
+template <> __device__ __forceinline__ ff canon<ff>(ff a) { return ff_canon(a); }
 
 // Conversion between accumulation types (ff <-> double <-> float).
 template <class To, class From> __device__ __forceinline__ To conv(From a);

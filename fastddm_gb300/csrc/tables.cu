@@ -404,12 +404,19 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
   L.Tpad = (int)align_up((size_t)r.T, 64 / es);
   L.Hpad = (int)(2 * ((r.H + 1) / 2));
   // stage 1-2 blocking: ~64 KB of shared memory per transform buffer; every
-  // transform is padded by one swizzle group (128 bytes)
-  const size_t target = 64 * 1024;
+  // transform is padded by one swizzle group (128 bytes).  FDDM_B200_ROWS_KB,
+  // FDDM_B200_COLS_KB and FDDM_B200_COLS_FRAMES override the targets (tuning).
+  auto env_int = [](const char* name, int dflt) {
+    const char* v = std::getenv(name);
+    const int x = v ? std::atoi(v) : 0;
+    return x > 0 ? x : dflt;
+  };
+  const size_t rows_target = (size_t)env_int("FDDM_B200_ROWS_KB", 64) * 1024;
+  const size_t cols_target = (size_t)env_int("FDDM_B200_COLS_KB", 64) * 1024;
   const size_t g = 128 / es;
-  L.pairs_per_block = (int)std::max<size_t>(1, std::min<size_t>(target / ((size_t)r.nx * es), (size_t)((r.H + 1) / 2)));
-  const int nb = (int)std::max<size_t>(1, target / ((size_t)r.ny * es));
-  L.frames_per_block = std::min(nb, 8);
+  L.pairs_per_block = (int)std::max<size_t>(1, std::min<size_t>(rows_target / ((size_t)r.nx * es), (size_t)((r.H + 1) / 2)));
+  const int nb = (int)std::max<size_t>(1, cols_target / ((size_t)r.ny * es));
+  L.frames_per_block = std::min(nb, env_int("FDDM_B200_COLS_FRAMES", 8));
   L.cols_per_block = std::max(1, nb / L.frames_per_block);
   auto cols_bytes = [&] {
     return (size_t)(2 * (L.frames_per_block * L.cols_per_block * (r.ny + g) + g)) * es;

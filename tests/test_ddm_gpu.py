@@ -363,3 +363,23 @@ def test_input_paths_agree(fddm, mode):
     np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(a, c)
     _check(a, imgs, lags, mode, "ff", label="input paths")
+
+
+@pytest.mark.parametrize("precision", ["ff", "f64", "f32"])
+@pytest.mark.parametrize("T", [4000, 2000, 700, 64, 3])
+def test_fused_radix2_temporal_path_is_bitwise_identical(fddm, monkeypatch, T, precision):
+    """Plans with first radix 2 fold the padded first pass into the pass over the series and run the
+    last forward pass, the pairing and the first inverse pass as one step: the same operations in
+    the same order.  Float-float arithmetic is written with explicitly rounded operations, so its
+    results equal those of the separate passes bit for bit; the native FP64 and FP32 tiers leave
+    multiply-add contraction to the compiler, which may differ between the two code paths."""
+    imgs = _poisson_stack((T, 6, 8), "uint16", seed=T)
+    lags = _long_lags(T, 25) if T > 40 else list(range(1, T))
+    fused = fddm.ddm(imgs, lags, mode="fft", precision=precision)._data
+    monkeypatch.setenv("FDDM_B200_TEMPORAL_FUSED", "0")
+    separate = fddm.ddm(imgs, lags, mode="fft", precision=precision)._data
+    if precision == "ff":
+        np.testing.assert_array_equal(fused, separate)
+    elif precision == "f64":
+        np.testing.assert_allclose(fused, separate, rtol=1e-11, atol=0.0)
+    _check(fused, imgs, lags, "fft", precision, label=f"fused T={T}")
