@@ -19,3 +19,18 @@ from .noise_est import estimate_camera_noise
 from . import lags, mask, utils, window
 
 __version__ = "0.1.0"
+
+
+def _load_tuning_table() -> None:
+    """Measured launch shapes of the temporal kernels (``tuning_table.json``), when the library is built."""
+    from . import _build, autotune
+
+    # only an up-to-date library: loading a stale one would keep it in the process across a rebuild
+    if _build.LIB_PATH.exists() and not _build.is_stale():
+        try:
+            autotune.load_table()
+        except (OSError, RuntimeError, ValueError, KeyError, AttributeError):  # no table: the occupancy model
+            pass
+
+
+_load_tuning_table()

@@ -353,10 +353,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
       if (!attach(ta.pt, 2) || !attach(ta.pt2, 3)) return 3;
       ta.slotA = d_slots; ta.slotB = d_slots + (T + 1);
       ta.need = ws + L.need_off;
-      const size_t with_need = temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), true);
-      ta.need_in_smem = with_need <= kSmemLimit ? 1 : 0;
-      smem_t = temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), ta.need_in_smem != 0);
-      threads = 0;  // chosen below by occupancy
+      threads = 0;  // chosen below (tuning table, autotuner or occupancy model)
     }
   } else if (!L.diff_staged) {
     smem_t = 96 * sizeof(A);
@@ -370,46 +367,138 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   int dev = 0, nsm = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  // CTA size of the shared-memory temporal kernels: the candidate that keeps the
-  // most warps resident per SM, the smallest such CTA on ties.  Each CTA works
-  // on its own mode, so several smaller CTAs per SM keep issuing while one of
-  // them waits at a barrier (measured on 512^2 stacks, 200 lags: 1.18x at
-  // T = 2000, 1.5x at T = 1000, 2.2x at T = 500 against one radix-8 butterfly
-  // per thread).  FDDM_B200_TEMPORAL_THREADS=128|256|512 overrides the choice.
-  auto pick_threads = [&](auto kernel) {
+  // Launch configuration of the temporal kernel: CTA size and, for the
+  // shared-memory fft kernel, whether the needed prefix sums and per-lag tables
+  // sit in shared memory (fewer resident CTAs) or in global scratch.
+  //  1. an entry of the tuning table (loaded from a committed table, or written
+  //     by the autotuner on an earlier call), else
+  //  2. with the autotuner on, every candidate is timed on this call's own
+  //     spectrum (a few waves of modes; their outputs are rewritten by the real
+  //     launch) and the fastest is recorded, else
+  //  3. the occupancy model: the most resident warps per SM, then the most
+  //     resident CTAs (smaller CTAs: each works on its own mode, so while one
+  //     waits at a barrier the others issue; measured on 512^2 stacks, 200
+  //     lags: 1.18x at T = 2000, 1.5x at T = 1000, 2.2x at T = 500 against one
+  //     radix-8 butterfly per thread), then shared-memory tables.
+  // FDDM_B200_TEMPORAL_THREADS=128|256|512 overrides the CTA size.
+  const bool shared_fft = r.mode == MODE_FFT && !long_fft;
+  const size_t with_need = shared_fft ? temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), true) : 0;
+  auto smem_of = [&](int nis) {
+    return shared_fft ? temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), nis != 0) : smem_t;
+  };
+  std::vector<TemporalChoice> cands;
+  for (int nis : {1, 0}) {
+    // the tables' placement only matters to the shared-memory fft kernel
+    if (shared_fft ? (nis == 1 && with_need > kSmemLimit) : nis == 1) continue;
+    for (int t : {512, 256, 128}) cands.push_back({t, nis});
+  }
+  auto occupancy = [&](auto kernel, const TemporalChoice& c) {
+    int o = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kernel, c.threads, smem_of(c.need_in_smem)) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return 0;
+    }
+    // the long-series kernel's per-CTA scratch holds kMaxLongCtas CTAs
+    if (long_fft) o = std::min(o, std::max(1, kMaxLongCtas / std::max(nsm, 1)));
+    return o;
+  };
+  const int tune_prec = tier_kind<S>::v == 0 ? PREC_FF : tier_kind<S>::v == 1 ? PREC_F64 : PREC_F32;
+  auto launch_range = [&](auto kernel, const TemporalChoice& c, size_t q0, size_t q1, unsigned grid) {
+    TemporalArgs t2 = ta;
+    t2.need_in_smem = c.need_in_smem;
+    t2.q_begin = q0;
+    t2.q_end = q1;
+    kernel<<<grid, c.threads, smem_of(c.need_in_smem), st>>>(t2);
+  };
+  auto choose = [&](auto kernel) -> bool {
+    for (const TemporalChoice& c : cands)
+      if ((ce = allow_smem(kernel, smem_of(c.need_in_smem))) != cudaSuccess) {
+        err = cudaGetErrorString(ce);
+        return false;
+      }
+    // the occupancy model's choice
+    TemporalChoice model{0, 0};
+    {
+      int best_w = 0, best_o = 0;
+      for (const TemporalChoice& c : cands) {
+        const int o = occupancy(kernel, c);
+        const int w = o * c.threads / 32;
+        if (o > 0 && (w > best_w || (w == best_w && o > best_o))) {
+          best_w = w;
+          best_o = o;
+          model = c;
+        }
+      }
+    }
+    TemporalChoice pick = model;
+    TemporalChoice tuned{0, 0};
+    const bool have = tuned_temporal(tune_prec, r.mode, T, nl, tuned) &&
+                      (!shared_fft ? tuned.need_in_smem == 0 : (tuned.need_in_smem == 0 || with_need <= kSmemLimit));
+    if (have) {
+      pick = tuned;
+    } else if (autotune_enabled()) {
+      // time every candidate on this call's spectrum (the real launch below
+      // rewrites these outputs); another candidate replaces the model's choice
+      // only when it is at least 3 % faster, so timing noise keeps the model
+      cudaEvent_t e0, e1;
+      if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+        // the same modes for every candidate: several waves of the largest grid
+        const size_t probe = std::min<size_t>(Q, 4 * (size_t)(long_fft ? kMaxLongCtas : kMaxTemporalCtas));
+        float best = 1e30f, model_ms = 1e30f;
+        TemporalChoice fastest = model;
+        bool ok = true;
+        for (const TemporalChoice& c : cands) {
+          const int o = occupancy(kernel, c);
+          if (o < 1) continue;
+          const size_t g = std::min<size_t>((size_t)o * nsm, long_fft ? kMaxLongCtas : kMaxTemporalCtas);
+          const unsigned grid = (unsigned)std::min(g, probe);
+          float ms = 1e30f;
+          launch_range(kernel, c, 0, probe, grid);  // warm-up
+          for (int rep = 0; rep < 3 && ok; ++rep) {  // the fastest of three timed launches
+            float m = 0.0f;
+            cudaEventRecord(e0, st);
+            launch_range(kernel, c, 0, probe, grid);
+            cudaEventRecord(e1, st);
+            ok = cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&m, e0, e1) == cudaSuccess;
+            if (ok) ms = std::min(ms, m);
+          }
+          count_launches(4);
+          if (!ok) break;
+          if (c.threads == model.threads && c.need_in_smem == model.need_in_smem) model_ms = ms;
+          if (ms < best) {
+            best = ms;
+            fastest = c;
+          }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (ok) {
+          pick = best < 0.97f * model_ms ? fastest : model;
+          record_temporal(tune_prec, r.mode, T, nl, pick);
+        }
+      }
+      if ((ce = cudaGetLastError()) != cudaSuccess) {
+        err = cudaGetErrorString(ce);
+        return false;
+      }
+    }
     if (const char* tt = std::getenv("FDDM_B200_TEMPORAL_THREADS")) {
       const int v = std::atoi(tt);
-      if (v == 128 || v == 256 || v == 512) return v;
+      if (v == 128 || v == 256 || v == 512) pick.threads = v;
     }
-    int best = 512, best_warps = 0;
-    for (int t : {512, 256, 128}) {
-      int o = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kernel, t, smem_t) != cudaSuccess) {
-        (void)cudaGetLastError();
-        continue;
-      }
-      // the long-series kernel's per-CTA scratch holds kMaxLongCtas CTAs
-      if (long_fft) o = std::min(o, std::max(1, kMaxLongCtas / std::max(nsm, 1)));
-      if (o * t / 32 >= best_warps && o > 0) {
-        best_warps = o * t / 32;
-        best = t;
-      }
-    }
-    return best;
-  };
-  auto prepare = [&](auto kernel) -> bool {
-    if ((ce = allow_smem(kernel, smem_t)) != cudaSuccess) { err = cudaGetErrorString(ce); return false; }
-    threads = pick_threads(kernel);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem_t);
+    threads = pick.threads;
+    ta.need_in_smem = pick.need_in_smem;
+    smem_t = smem_of(pick.need_in_smem);
+    occ = occupancy(kernel, pick);
     return true;
   };
   bool prepared;
-  if (long_fft) prepared = prepare(k_tfft_long<S, A>);
+  if (long_fft) prepared = choose(k_tfft_long<S, A>);
   else if (r.mode == MODE_FFT)
-    prepared = f2t ? prepare(tfft_kernel<S, A, true, true>())
-                   : p2t ? prepare(tfft_kernel<S, A, true>()) : prepare(tfft_kernel<S, A, false>());
-  else if (L.diff_staged) prepared = prepare(k_tdiff<S, A, true>);
-  else prepared = prepare(k_tdiff<S, A, false>);
+    prepared = f2t ? choose(tfft_kernel<S, A, true, true>())
+                   : p2t ? choose(tfft_kernel<S, A, true>()) : choose(tfft_kernel<S, A, false>());
+  else if (L.diff_staged) prepared = choose(k_tdiff<S, A, true>);
+  else prepared = choose(k_tdiff<S, A, false>);
   if (!prepared) return 3;
   if (occ < 1) { err = "temporal kernel does not fit on an SM (shared memory " + std::to_string(smem_t) + " B)"; return 4; }
   const size_t max_grid = std::min<size_t>((size_t)occ * nsm, long_fft ? kMaxLongCtas : kMaxTemporalCtas);

@@ -143,6 +143,17 @@ constexpr size_t kSmemLimit = 232448;  // 227 KB opt-in per CTA
 // Shared memory of the long-series fft-mode kernel (sub-transforms of length M1).
 size_t temporal_long_smem(int M1, size_t es, size_t ea);
 
+// Launch configuration of a temporal kernel (CTA size; the needed prefix sums
+// and per-lag tables in shared memory or in global scratch), and the tuning
+// table the autotuner fills (tune.cu), keyed by (precision, mode, T, nlags).
+struct TemporalChoice {
+  int threads;
+  int need_in_smem;
+};
+bool tuned_temporal(int precision, int mode, int64_t T, int64_t nlags, TemporalChoice& out);
+void record_temporal(int precision, int mode, int64_t T, int64_t nlags, const TemporalChoice& c);
+bool autotune_enabled();
+
 // Thread-local error message reported by fddm_b200_last_error().
 void set_last_error(const std::string& msg);
 int fail_with(int code, const std::string& msg);

@@ -254,6 +254,25 @@ int fddm_b200_polyfit_noise(const double* d_data, uint64_t ld, uint64_t npix, co
 int fddm_b200_tiff_info(const char* path, uint64_t* npages, uint64_t* height, uint64_t* width, int* dtype);
 int fddm_b200_tiff_read(const char* path, const uint64_t* pages, uint64_t npages, void* dst, int nthreads);
 
+/* Launch tuning of the temporal kernels (no counterpart in the reference,
+   which has fixed launch shapes; its memory planner, src/cuda/memchk_gpu.cu:141-702,
+   only sizes chunks).  A problem class is (precision, mode, length, nlags);
+   its entry holds the CTA size (128, 256 or 512 threads) and whether the
+   needed prefix sums and per-lag tables sit in shared memory (need_in_smem=1)
+   or in global scratch.  Without an entry the library uses its occupancy
+   model; with fddm_b200_set_autotune(1), the first call of a class without an
+   entry times every candidate on that call's own spectrum (the call then
+   waits for the GPU once) and records the fastest.  Entries only change the
+   launch shape and the order of the per-mode sums (results within rounding
+   of each other; every call of one class in a process uses the same entry).
+   fddm_b200_tuning_count / _entry enumerate the table (for saving it). */
+int fddm_b200_set_autotune(int enable);
+int fddm_b200_tuning_set(int precision, int mode, uint64_t length, uint64_t nlags, int threads, int need_in_smem);
+int fddm_b200_tuning_get(int precision, int mode, uint64_t length, uint64_t nlags, int* threads, int* need_in_smem);
+uint64_t fddm_b200_tuning_count(void);
+int fddm_b200_tuning_entry(uint64_t index, int* precision, int* mode, uint64_t* length, uint64_t* nlags, int* threads,
+                           int* need_in_smem);
+
 /* Diagnostics (no counterpart in the reference, which has no tracing).
    fddm_b200_set_stage_timing(1) makes every following ddm call record CUDA
    events on its stream around the spatial stage (row and column FFT passes)
