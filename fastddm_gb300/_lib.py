@@ -91,6 +91,12 @@ _SIGNATURES = {
     "fddm_b200_batch_run": (
         ctypes.c_int, [ctypes.POINTER(Job), ctypes.c_uint64, ctypes.c_int, _vp, ctypes.c_size_t, _vp]
     ),
+    "fddm_b200_batch_create": (
+        ctypes.c_int,
+        [ctypes.POINTER(Job), ctypes.c_uint64, ctypes.c_int, _vp, ctypes.c_size_t, _vp, ctypes.POINTER(_vp)],
+    ),
+    "fddm_b200_batch_launch": (ctypes.c_int, [_vp, _vp]),
+    "fddm_b200_batch_destroy": (ctypes.c_int, [_vp]),
     "fddm_b200_set_stage_timing": (ctypes.c_int, [ctypes.c_int]),
     "fddm_b200_stage_times": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "fddm_b200_launch_count": (ctypes.c_uint64, []),

@@ -2,9 +2,11 @@
 
 ``ddm_batch`` validates every stack like ``ddm()`` (lags sorted and
 deduplicated, lag 0 dropped with a warning, window shape checked) and runs all
-of them through ``fddm_b200_batch_run``: one workspace, jobs scheduled
-longest-first over library-owned streams so that independent stacks overlap
-on the GPU.  Each result equals the one ``ddm()`` gives for that stack alone.
+of them as one prepared batch (``fddm_b200_batch_create`` / ``_launch``): one
+workspace, spatial stages scheduled longest-first over library-owned streams,
+and the temporal stages of all stacks in one persistent launch of the
+many-job kernel per kernel variant and CTA size.  Each result equals the one
+``ddm()`` gives for that stack alone.
 """
 
 from __future__ import annotations
@@ -59,14 +61,24 @@ class BatchJob:
 
 
 class BatchPlan:
-    """Workspace and job table for a fixed list of jobs; can be run repeatedly."""
+    """Workspace, job table and prepared library plan for a fixed list of jobs; can be run repeatedly.
 
-    def __init__(self, jobs: List[BatchJob], precision: str = "ff", device=None):
+    Creating the plan queues every job's tables into the workspace and sets
+    up the temporal stages (``fddm_b200_batch_create``); :meth:`run` enqueues
+    the batch's kernels only (``fddm_b200_batch_launch``).  With
+    ``graph=True`` the first run also captures that launch into a CUDA graph
+    and every later run replays the graph.
+    """
+
+    def __init__(self, jobs: List[BatchJob], precision: str = "ff", device=None, graph: bool = False):
         if torch is None or not torch.cuda.is_available():
             raise RuntimeError("the b200 batch needs a CUDA device (GB300)")
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         self.precision = precision
         self.jobs = jobs
+        self._plan = None
+        self._use_graph = graph
+        self._graph = None
         self._table = (_lib.Job * max(1, len(jobs)))()
         for i, j in enumerate(jobs):
             T, H, W = j.shape
@@ -87,22 +99,52 @@ class BatchPlan:
         size = ctypes.c_size_t(0)
         with torch.cuda.device(self.device):
             _lib.check(lib.fddm_b200_batch_workspace_size(self._table, len(jobs), _lib.PREC[precision], ctypes.byref(size)))
-        self.workspace_bytes = int(size.value)
-        free, _ = torch.cuda.mem_get_info(self.device)
-        cached = torch.cuda.memory_reserved(self.device) - torch.cuda.memory_allocated(self.device)
-        if self.workspace_bytes > 0.9 * (free + cached):
-            raise RuntimeError("Not enough memory")
-        self.workspace = torch.empty(max(1, self.workspace_bytes), dtype=torch.uint8, device=self.device)
+            self.workspace_bytes = int(size.value)
+            free, _ = torch.cuda.mem_get_info(self.device)
+            cached = torch.cuda.memory_reserved(self.device) - torch.cuda.memory_allocated(self.device)
+            if self.workspace_bytes > 0.9 * (free + cached):
+                raise RuntimeError("Not enough memory")
+            self.workspace = torch.empty(max(1, self.workspace_bytes), dtype=torch.uint8, device=self.device)
+            handle = ctypes.c_void_p()
+            self._stream = torch.cuda.current_stream(self.device)
+            _lib.check(lib.fddm_b200_batch_create(self._table, len(jobs), _lib.PREC[precision],
+                                                  self.workspace.data_ptr(), self.workspace_bytes,
+                                                  self._stream.cuda_stream, ctypes.byref(handle)))
+            self._plan = handle
+
+    def _launch(self, stream) -> None:
+        _lib.check(_lib.load().fddm_b200_batch_launch(self._plan, stream.cuda_stream))
 
     def run(self, stream=None) -> List["torch.Tensor"]:
         """Enqueue the whole batch on `stream` (default: current); returns the output tensors."""
-        lib = _lib.load()
         if stream is None:
             stream = torch.cuda.current_stream(self.device)
         with torch.cuda.device(self.device):
-            _lib.check(lib.fddm_b200_batch_run(self._table, len(self.jobs), _lib.PREC[self.precision],
-                                               self.workspace.data_ptr(), self.workspace_bytes, stream.cuda_stream))
+            if stream != self._stream:
+                stream.wait_stream(self._stream)  # the tables queued at creation
+            if not self._use_graph:
+                self._launch(stream)
+            else:
+                if self._graph is None:
+                    self._launch(stream)  # first run outside capture: kernel attributes and caches settle
+                    g = torch.cuda.CUDAGraph()
+                    side = torch.cuda.Stream(self.device)
+                    side.wait_stream(stream)
+                    with torch.cuda.graph(g, stream=side, capture_error_mode="relaxed"):
+                        self._launch(side)
+                    stream.wait_stream(side)
+                    self._graph = g
+                with torch.cuda.stream(stream):
+                    self._graph.replay()
         return [j.out for j in self.jobs]
+
+    def __del__(self):
+        if getattr(self, "_plan", None) is not None:
+            try:
+                _lib.load().fddm_b200_batch_destroy(self._plan)
+            except Exception:  # interpreter shutdown: the library may already be unloaded
+                pass
+            self._plan = None
 
 
 def make_job(img_seq, lags, *, mode: str = "fft", window=None, device=None) -> BatchJob:

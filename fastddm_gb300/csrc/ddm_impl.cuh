@@ -523,8 +523,9 @@ __device__ __forceinline__ void last_pass_pair_first_inverse(cx<S>* __restrict__
 // or 8 (host: fused_radix2_ok).  The padded radix-2 first pass is folded into
 // the pass over the series (G at t and G w_N^t at N/2 + t), and the last
 // forward pass, the pairing and the first inverse pass run as one step.
+// Modes q_first, q_first + q_step, ... below q_stop of the job described by `a`.
 template <class S, class A, bool P2, bool F2 = false>
-__device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
+__device__ __forceinline__ void tfft_body(const TemporalArgs& a, size_t q_first, size_t q_stop, size_t q_step) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int T = a.T, N = a.nt, N2 = a.nt / 2, nl = a.nlags;
   cx<S>* buf = reinterpret_cast<cx<S>*>(smem_raw);
@@ -567,9 +568,9 @@ __device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
       FDDM_LAG_W[l] = tw[tau];
     }
   }
-  if (a.q_begin + blockIdx.x < a.q_end) prefetch_series<S>(ser, F + (a.q_begin + blockIdx.x) * a.Tpad, T, tid, nthr);
+  if (q_first < q_stop) prefetch_series<S>(ser, F + q_first * a.Tpad, T, tid, nthr);
 
-  for (size_t q = a.q_begin + blockIdx.x; q < a.q_end; q += gridDim.x) {
+  for (size_t q = q_first; q < q_stop; q += q_step) {
     cp_async_wait_all();
     __syncthreads();
 
@@ -639,7 +640,7 @@ __device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
       else if (R == 4) last_pass_pair_first_inverse<S, 4>(buf, N2, tid, nthr);
       else last_pass_pair_first_inverse<S, 2>(buf, N2, tid, nthr);
       __syncthreads();
-      if (q + gridDim.x < a.q_end) prefetch_series<S>(ser, F + (q + gridDim.x) * a.Tpad, T, tid, nthr);
+      if (q + q_step < q_stop) prefetch_series<S>(ser, F + (q + q_step) * a.Tpad, T, tid, nthr);
       // remaining inverse passes of the half plan (its last pass ran above)
       for (int s = a.pt2.npass - 2; s >= 0; --s) {
         fft_pass_dispatch<S, true, true>(buf, 1, N2, a.pt2, s, tw, N, tid, nthr);
@@ -652,7 +653,7 @@ __device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
       else pair_power<S, 2>(buf, M1, tid, nthr);
       __syncthreads();
       // buf above the half-length transform is free: start loading the next mode
-      if (q + gridDim.x < a.q_end) prefetch_series<S>(ser, F + (q + gridDim.x) * a.Tpad, T, tid, nthr);
+      if (q + q_step < q_stop) prefetch_series<S>(ser, F + (q + q_step) * a.Tpad, T, tid, nthr);
       // the length-N table serves the half-length passes: w_M^k = tw[k N / M]
       fft_inverse<S, P2>(buf, 1, N2, a.pt2, tw, tid, nthr, N);
     }
@@ -711,12 +712,53 @@ __device__ __forceinline__ void tfft_body(const TemporalArgs& a) {
 
 template <class S, class A, bool P2, bool F2 = false>
 __global__ void __launch_bounds__(512) k_tfft(TemporalArgs a) {
-  tfft_body<S, A, P2, F2>(a);
+  tfft_body<S, A, P2, F2>(a, a.q_begin + blockIdx.x, a.q_end, gridDim.x);
 }
 // FP32 transforms: two 512-thread CTAs per SM (their shared memory allows it)
 template <class S, class A, bool P2, bool F2 = false>
 __global__ void __launch_bounds__(512, 2) k_tfft_x2(TemporalArgs a) {
-  tfft_body<S, A, P2, F2>(a);
+  tfft_body<S, A, P2, F2>(a, a.q_begin + blockIdx.x, a.q_end, gridDim.x);
+}
+
+// Many jobs in one persistent launch: CTAs take work items (a run of
+// consecutive modes of one job) from a counter in global memory, copy the
+// job's arguments to shared memory and run the same per-mode body as k_tfft,
+// so every mode gives the result it gives in a launch of its own job.  The
+// counter starts at zero (set by the host before the launch); taking an item
+// is one atomic add, and no CTA ever waits on another.
+template <class S, class A, bool P2, bool F2>
+__device__ __forceinline__ void tfft_list_body(const TemporalArgs* __restrict__ jobs,
+                                               const TemporalItem* __restrict__ items, int nitems,
+                                               int* __restrict__ counter) {
+  __shared__ __align__(16) TemporalArgs s_args;
+  __shared__ int s_item;
+  constexpr int kWords = (int)(sizeof(TemporalArgs) / sizeof(int));
+  static_assert(sizeof(TemporalArgs) % sizeof(int) == 0, "TemporalArgs copied as ints");
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= nitems) break;
+    const TemporalItem w = items[it];
+    const int* src = reinterpret_cast<const int*>(jobs + w.job);
+    int* dst = reinterpret_cast<int*>(&s_args);
+    for (int i = threadIdx.x; i < kWords; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    tfft_body<S, A, P2, F2>(s_args, (size_t)w.q0, (size_t)w.q1, 1);
+    __syncthreads();
+  }
+}
+template <class S, class A, bool P2, bool F2 = false>
+__global__ void __launch_bounds__(512) k_tfft_list(const TemporalArgs* __restrict__ jobs,
+                                                   const TemporalItem* __restrict__ items, int nitems,
+                                                   int* __restrict__ counter) {
+  tfft_list_body<S, A, P2, F2>(jobs, items, nitems, counter);
+}
+template <class S, class A, bool P2, bool F2 = false>
+__global__ void __launch_bounds__(512, 2) k_tfft_list_x2(const TemporalArgs* __restrict__ jobs,
+                                                         const TemporalItem* __restrict__ items, int nitems,
+                                                         int* __restrict__ counter) {
+  tfft_list_body<S, A, P2, F2>(jobs, items, nitems, counter);
 }
 
 // ---------------------------------------------------------------------------

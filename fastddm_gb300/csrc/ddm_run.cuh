@@ -199,19 +199,22 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
 
   // window in the FFT scalar type
   const void* win_s = nullptr;
-  if (r.window) {
+  const bool do_spatial = (r.stages & 1) != 0;
+  if (r.window && do_spatial) {
     S* w = reinterpret_cast<S*>(ws + L.win_off);
     const size_t n = (size_t)H * W;
     k_window_convert<S><<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, st>>>(r.window, w, n);
     if ((ce = cudaGetLastError()) != cudaSuccess) { err = cudaGetErrorString(ce); return 3; }
     win_s = w;
+  } else if (r.window) {
+    win_s = ws + L.win_off;
   }
   // lags and reciprocal normalisations
   std::vector<double> rcp(nl);
   for (int l = 0; l < nl; ++l) rcp[l] = 1.0 / (double)(T - r.lags[l]);
   int* d_lags = reinterpret_cast<int*>(ws + L.lags_off);
   double* d_rcp = reinterpret_cast<double*>(ws + L.rcp_off);
-  if (nl > 0) {
+  if (nl > 0 && !r.tables_ready) {
     if ((ce = cudaMemcpyAsync(d_lags, r.lags.data(), nl * sizeof(int), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
         (ce = cudaMemcpyAsync(d_rcp, rcp.data(), nl * sizeof(double), cudaMemcpyHostToDevice, st)) != cudaSuccess) {
       err = cudaGetErrorString(ce);
@@ -220,7 +223,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   }
   // slot tables of the prefix sums each lag needs: pfx[T - lag] (A) and pfx[lag] (B)
   int* d_slots = reinterpret_cast<int*>(ws + L.slot_off);
-  if (r.mode == MODE_FFT && !L.long_R0) {
+  if (r.mode == MODE_FFT && !L.long_R0 && !r.tables_ready) {
     std::vector<int> slots(2 * (size_t)(T + 1), -1);
     for (int l = 0; l < nl; ++l) {
       slots[T - r.lags[l]] = l;
@@ -232,9 +235,9 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     }
   }
 
-  StageEvents* evs = r.inline_tables ? nullptr : stage_events();
+  StageEvents* evs = (r.inline_tables || r.stages != 3 || r.collect) ? nullptr : stage_events();
   if (evs) cudaEventRecord(evs->ev[0], st);
-  int launches = r.window ? 1 : 0;
+  int launches = r.window && do_spatial ? 1 : 0;
 
 
 
@@ -294,7 +297,7 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
       return 3;
     }
   }
-  for (int t0 = 0; t0 < T; t0 += L.chunk) {
+  for (int t0 = 0; do_spatial && t0 < T; t0 += L.chunk) {
     sa.t0 = t0;
     sa.tc = std::min(L.chunk, T - t0);
     if (upload) {
@@ -321,6 +324,10 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     launches += 2;
   }
   if (evs) cudaEventRecord(evs->ev[1], st);
+  if (!(r.stages & 2) && !r.collect) {
+    count_launches(launches);
+    return 0;
+  }
 
   // stage 3
   TemporalArgs ta{};
@@ -501,6 +508,16 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   else prepared = choose(k_tdiff<S, A, false>);
   if (!prepared) return 3;
   if (occ < 1) { err = "temporal kernel does not fit on an SM (shared memory " + std::to_string(smem_t) + " B)"; return 4; }
+  if (r.collect) {  // the caller launches this stage (the many-job kernel, or on its own later)
+    ta.q_begin = 0;
+    ta.q_end = Q;
+    r.collect->args = ta;
+    r.collect->threads = threads;
+    r.collect->smem = smem_t;
+    r.collect->variant = (r.mode == MODE_FFT && !long_fft) ? (f2t ? 2 : p2t ? 1 : 0) : -1;
+    count_launches(launches);
+    return 0;
+  }
   const size_t max_grid = std::min<size_t>((size_t)occ * nsm, long_fft ? kMaxLongCtas : kMaxTemporalCtas);
   // With a host result the modes run in chunks: each chunk's output columns
   // (all lag rows) go to the host with a 2D copy on the copy stream while the
@@ -551,6 +568,49 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     }
   }
   return 0;
+}
+
+// One launch of the many-job temporal kernel over the items of group `g`.
+template <class S, class A>
+int run_temporal_list_t(const TemporalListGroup& g, cudaStream_t st, std::string& err) {
+  if (g.nitems <= 0) return 0;
+  auto go = [&](auto kernel) -> int {
+    cudaError_t ce = allow_smem(kernel, g.smem);
+    int occ = 0, dev = 0, nsm = 0;
+    if (ce == cudaSuccess) ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, g.threads, g.smem);
+    if (ce == cudaSuccess) ce = cudaGetDevice(&dev);
+    if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (ce != cudaSuccess) {
+      err = cudaGetErrorString(ce);
+      return 3;
+    }
+    if (occ < 1) {
+      err = "many-job temporal kernel does not fit on an SM (shared memory " + std::to_string(g.smem) + " B)";
+      return 4;
+    }
+    const unsigned grid =
+        (unsigned)std::min<size_t>(std::min<size_t>((size_t)occ * nsm, kMaxTemporalCtas), (size_t)g.nitems);
+    if ((ce = cudaMemsetAsync(g.d_counter, 0, sizeof(int), st)) != cudaSuccess) {
+      err = cudaGetErrorString(ce);
+      return 3;
+    }
+    kernel<<<grid, g.threads, g.smem, st>>>(g.d_args, g.d_items, g.nitems, g.d_counter);
+    if ((ce = cudaGetLastError()) != cudaSuccess) {
+      err = cudaGetErrorString(ce);
+      return 3;
+    }
+    count_launches(1);
+    return 0;
+  };
+  if constexpr (sizeof(S) == 4) {
+    if (g.variant == 2) return go(k_tfft_list_x2<S, A, true, true>);
+    if (g.variant == 1) return go(k_tfft_list_x2<S, A, true, false>);
+    return go(k_tfft_list_x2<S, A, false, false>);
+  } else {
+    if (g.variant == 2) return go(k_tfft_list<S, A, true, true>);
+    if (g.variant == 1) return go(k_tfft_list<S, A, true, false>);
+    return go(k_tfft_list<S, A, false, false>);
+  }
 }
 
 }  // namespace fddm

@@ -72,6 +72,34 @@ struct TemporalArgs {
   size_t xs_pfx_off;      // offset of the prefix sums inside one CTA's scratch
 };
 
+// A work item of the many-job temporal kernel (k_tfft_list): modes q0 .. q1 - 1 of job `job`.
+struct TemporalItem {
+  int job;
+  int pad;
+  unsigned long long q0, q1;
+};
+
+// The temporal stage of one job, set up but not launched (DdmRequest::collect):
+// its arguments and launch shape, and whether the many-job kernel can run it
+// (the shared-memory fft kernel; variant 0 generic, 1 radices 2/4/8, 2 the
+// fused radix-2 path; -1 other kernels).
+struct TemporalLaunch {
+  TemporalArgs args;
+  int threads = 0;
+  size_t smem = 0;
+  int variant = -1;
+};
+
+// One launch of the many-job temporal kernel: jobs of one variant and CTA size.
+struct TemporalListGroup {
+  int variant = 0, threads = 0;
+  size_t smem = 0;              // dynamic shared memory (the largest of the group's jobs)
+  const TemporalArgs* d_args = nullptr;
+  const TemporalItem* d_items = nullptr;
+  int nitems = 0;
+  int* d_counter = nullptr;     // zeroed on the launch stream before the launch
+};
+
 enum Precision { PREC_FF = 0, PREC_F64 = 1, PREC_F32 = 2 };
 enum Mode { MODE_FFT = 0, MODE_DIFF = 1 };
 enum DType { DT_U8 = 0, DT_I16 = 1, DT_U16 = 2, DT_I32 = 3, DT_U32 = 4, DT_I64 = 5, DT_U64 = 6, DT_F32 = 7, DT_F64 = 8 };
@@ -98,6 +126,13 @@ struct DdmRequest {
   // the spatial passes that read it; host_out (optional) receives the result.
   const void* host_img = nullptr;
   double* host_out = nullptr;
+  // Batched use: the lag, normalisation and slot tables are already in the
+  // workspace (put there by an earlier call of the same request), `stages`
+  // selects the spatial (1) and temporal (2) launches, and a non-null
+  // `collect` receives the temporal stage's arguments instead of a launch.
+  bool tables_ready = false;
+  int stages = 3;
+  TemporalLaunch* collect = nullptr;
 };
 
 // Per-device copy stream and event used to overlap frame uploads with compute.
@@ -188,6 +223,12 @@ bool temporal_plan(int n, FftPlan& p);
 int run_ddm_ff(const DdmRequest& r, cudaStream_t st, std::string& err);
 int run_ddm_f64(const DdmRequest& r, cudaStream_t st, std::string& err);
 int run_ddm_f32(const DdmRequest& r, cudaStream_t st, std::string& err);
+// One launch of the many-job temporal kernel (zeroes the group's counter first).
+int run_temporal_list_ff(const TemporalListGroup& g, cudaStream_t st, std::string& err);
+int run_temporal_list_f64(const TemporalListGroup& g, cudaStream_t st, std::string& err);
+int run_temporal_list_f32(const TemporalListGroup& g, cudaStream_t st, std::string& err);
+// Static shared memory of the many-job kernel (its copy of the job's arguments).
+constexpr size_t kListStaticSmem = sizeof(TemporalArgs) + 64;
 
 // Attach the cached per-device pass twiddle tables of `p` (kind as get_tables).
 bool attach_pass_tables(FftPlan& p, int kind, std::string& err);

@@ -144,15 +144,32 @@ typedef struct fddm_b200_job {
   double* d_out;            /* (nlags + 2, ny, nx/2 + 1) */
 } fddm_b200_job;
 
-/* Workspace bytes of fddm_b200_batch_run for these jobs (sum of the jobs' own
-   workspaces, 256-byte aligned). */
+/* Workspace bytes of a batch of these jobs (the jobs' own workspaces, 256-byte
+   aligned, and the tables of the many-job temporal kernel). */
 int fddm_b200_batch_workspace_size(const fddm_b200_job* jobs, uint64_t njobs, int precision, size_t* bytes);
 
-/* Run all jobs.  Every job is validated before anything is launched; the jobs
-   are then scheduled longest-first onto library-owned streams forked from
-   `stream` and joined back into it, so the batch completes in stream order
-   while independent jobs overlap on the GPU.  Each job's result is identical
-   to running it alone. */
+/* A prepared batch.  fddm_b200_batch_create validates every job, puts each
+   job's lag and slot tables into its part of d_workspace and sets up every
+   temporal stage (queued on `stream`; the launch tuning of each job's class is
+   resolved here, which may time candidates once when the autotuner is on).
+   fddm_b200_batch_launch then enqueues kernels and event dependencies only, so
+   a stream capture of it gives a CUDA graph of the whole batch:
+     - the spatial stages, longest first, onto library-owned streams forked
+       from `stream`;
+     - the temporal stages of all fft-mode jobs as one persistent launch of a
+       many-job kernel per kernel variant and CTA size, whose CTAs take runs of
+       32 modes of any job from a counter (the other stages launch per job);
+     - a join back into `stream`, so the batch completes in stream order.
+   The frames, windows and outputs of the jobs and d_workspace must stay valid
+   for the plan's life; launch on `stream` (or after the create's work on it
+   has completed).  Each job's result is identical to running it alone. */
+typedef struct fddm_b200_batch fddm_b200_batch;
+int fddm_b200_batch_create(const fddm_b200_job* jobs, uint64_t njobs, int precision, void* d_workspace,
+                           size_t workspace_bytes, void* stream, fddm_b200_batch** plan);
+int fddm_b200_batch_launch(fddm_b200_batch* plan, void* stream);
+int fddm_b200_batch_destroy(fddm_b200_batch* plan);
+
+/* Create, launch and destroy in one call. */
 int fddm_b200_batch_run(const fddm_b200_job* jobs, uint64_t njobs, int precision, void* d_workspace,
                         size_t workspace_bytes, void* stream);
 

@@ -41,6 +41,30 @@ def test_batch_equals_single_calls(fddm, mode):
         np.testing.assert_array_equal(r.ky, alone.ky)
 
 
+def test_batch_graph_replay_equals_single_calls(fddm):
+    """The batch captured into a CUDA graph: every replay rewrites each output with the single-call result,
+    windowed and unwindowed stacks of several temporal kernel variants in one many-job launch per group."""
+    import torch
+
+    from fastddm_gb300.batch import BatchPlan, make_job
+
+    dev = torch.device("cuda", 0)
+    stacks = _stacks()
+    lags = [np.arange(1, s.shape[0]) for s in stacks]
+    windows = [fddm.window.blackman_harris(s.shape) if i % 2 else None for i, s in enumerate(stacks)]
+    jobs = [make_job(s, lg, window=w, device=dev) for s, lg, w in zip(stacks, lags, windows)]
+    plan = BatchPlan(jobs, "ff", dev, graph=True)
+    alone = [fddm.ddm(s, lg, mode="fft", window=w)._data for s, lg, w in zip(stacks, lags, windows)]
+    for _ in range(3):  # capture, then replays
+        for j in jobs:
+            j.out.fill_(float("nan"))
+        outs = plan.run()
+        torch.cuda.synchronize()
+        for o, a in zip(outs, alone):
+            np.testing.assert_array_equal(o.cpu().numpy(), a)
+    assert plan._graph is not None
+
+
 def test_batch_rejects_an_invalid_job_before_running(fddm):
     from fastddm_gb300 import _lib
     from fastddm_gb300.batch import BatchPlan, make_job
