@@ -557,6 +557,12 @@ def run_ours(args):
                "sample": f"spatial FFT of 32 frames and the temporal stage of 16384 mode columns x {T} frames "
                          f"(FP64 numpy restatement of the cpp core), extrapolated to the full job"}
 
+    serve = None
+    if rank == 0 and ws == 1 and not args.no_serve and args.config == "large":
+        del frames
+        torch.cuda.empty_cache()
+        serve = serve_records(args, args.requests, device)
+
     if rank == 0:
         line = {
             "metric": "DDM frames/s", "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
@@ -565,7 +571,7 @@ def run_ours(args):
             "data": "synthetic", "config": workload_desc(args.config, scene, lags, args.precision, args.mode),
             "roofline": roofline, "issue_roofline": issue, "cpu_baseline": cpu, "e2e": e2e,
             "e2e_pageable": e2e_pageable, "accuracy": accuracy,
-            "max_rel_err": accuracy["max_rel_err"] if accuracy else None, "f64_path": f64,
+            "max_rel_err": accuracy["max_rel_err"] if accuracy else None, "f64_path": f64, "serve": serve,
             "clocks": clocks, "gpu_launches": launches,
         }
         print(json.dumps(line))
@@ -720,17 +726,15 @@ def run_batch(args):
     print(json.dumps(line))
 
 
-def run_serve(args):
-    """Poisson arrivals (50 req/s) of config-4-sized jobs plus 5 % 1024^2 x 2000 jobs."""
+def serve_records(args, n_req: int, device) -> dict:
+    """Poisson arrivals (50 req/s) of config-4-sized jobs plus 5 % 1024^2 x 2000 jobs, served twice:
+    continuous batching in the float-float tier, and one request at a time in the FP64 tier."""
     import torch
 
-    from fastddm_gb300 import _build, synthetic
+    from fastddm_gb300 import synthetic
     from fastddm_gb300._ddm_b200 import DdmPlan
     from fastddm_gb300.serving import DdmServer, GpuExecutor, Request, latency_summary, replay
 
-    _build.build()
-    device = torch.device("cuda", 0)
-    n_req = args.requests
     rng = np.random.default_rng(7)
     scenes = synthetic.config4_scenes(n_req, seed=100)
     big = rng.random(n_req) < 0.05
@@ -740,6 +744,7 @@ def run_serve(args):
     frames = [synthetic.make_stack_torch(sc, device=device) for sc in scenes]
     torch.cuda.synchronize(device)
     total_frames = sum(sc.length for sc in scenes)
+    checked = list(range(0, n_req, max(1, n_req // 8)))[:8]
 
     def requests():
         return [Request(i, frames[i], np.arange(1, scenes[i].length), "fft", None, float(arrivals[i]))
@@ -749,8 +754,9 @@ def run_serve(args):
     for label, prec, streams in (("continuous_batching", args.precision, 6), ("one_at_a_time_f64", "f64", 1)):
         torch.cuda.empty_cache()
         free, _ = torch.cuda.mem_get_info(device)
-        ex = GpuExecutor(0, prec, streams)
-        server = DdmServer(ex, int(0.85 * free))
+        ex = GpuExecutor(0, prec, streams, pool_bytes=int(0.35 * free))
+        server = DdmServer(ex, int(0.85 * free), small_bytes=64 << 20) if streams > 1 else \
+            DdmServer(ex, int(0.85 * free), small_bytes=0)
         # warm-up: FFT tables of every frame size and every temporal length in the stream
         for side in sorted({sc.height for sc in scenes}):
             p = DdmPlan("fft", 8, side, side, 2, np.arange(1, 8), side, side, 16, False, prec, device)
@@ -762,33 +768,55 @@ def run_serve(args):
             p.run(f, None, torch.empty(p.out_shape, dtype=torch.float64, device=device))
         torch.cuda.synchronize(device)
         ex.clock_start()
-        reqs = replay(server, requests(), time.perf_counter)
+        kept = {}
+
+        def deliver(r):  # the client takes each result; a few are kept for the identity check
+            res = server.fetch(r.rid)
+            if r.rid in checked and label == "continuous_batching":
+                kept[r.rid] = res
+
+        reqs = replay(server, requests(), time.perf_counter, deliver=deliver)
         span = max(r.completed for r in reqs) - min(r.arrival for r in reqs)
         summ = latency_summary(reqs)
-        summ.update({"frames_per_s": total_frames / span, "span_s": span, "peak_inflight": server.peak_inflight})
+        summ.update({"frames_per_s": total_frames / span, "span_s": span, "peak_inflight": server.peak_inflight,
+                     "batched_launches": server.batches, "slots": streams, "precision": prec})
         results[label] = summ
         if label == "continuous_batching":
             # a few results again, each alone on an idle device: must be identical
             same = True
-            for i in list(range(0, n_req, max(1, n_req // 8)))[:8]:
+            for i in checked:
                 sc = scenes[i]
                 p = DdmPlan("fft", sc.length, sc.height, sc.width, 2, np.arange(1, sc.length), sc.width, sc.height,
                             2 * sc.length, False, prec, device)
                 alone = torch.empty(p.out_shape, dtype=torch.float64, device=device)
                 p.run(frames[i], None, alone)
                 torch.cuda.synchronize(device)
-                mixed = server.finished[i].result
-                same = same and bool(torch.equal(alone, mixed))
+                same = same and bool(torch.equal(alone, kept[i]))
                 del p, alone
             results[label]["identical_alone_and_in_mix"] = same
-        del server, ex, reqs
-    cb = results["continuous_batching"]
+        del server, ex, reqs, kept
+    del frames
+    torch.cuda.empty_cache()
+    cb, one = results["continuous_batching"], results["one_at_a_time_f64"]
+    return {"requests": n_req, "arrivals": "Poisson, mean 50 requests/s", "large_jobs": int(big.sum()),
+            "frames": total_frames, "mode": "fft", "all_lags": True,
+            "p50_ms": cb["p50_ms"], "p99_ms": cb["p99_ms"], "frames_per_s": cb["frames_per_s"],
+            "vs_one_at_a_time_f64_frames_per_s": cb["frames_per_s"] / one["frames_per_s"], "legs": results}
+
+
+def run_serve(args):
+    import torch
+
+    from fastddm_gb300 import _build
+
+    _build.build()
+    rec = serve_records(args, args.requests, torch.device("cuda", 0))
     line = {
-        "metric": "serve p50/p99 latency", "value": cb["p99_ms"], "unit": "ms (p99)", "n_gpus": 1,
+        "metric": "serve p50/p99 latency", "value": rec["p99_ms"], "unit": "ms (p99)", "n_gpus": 1,
         "higher_is_better": False, "dtype": args.precision, "data": "synthetic",
-        "config": {"workload": f"serve_{n_req}_requests_poisson_50_per_s", "requests": n_req,
-                   "large_jobs": int(big.sum()), "frames": total_frames, "mode": "fft"},
-        "serve": results,
+        "config": {"workload": f"serve_{args.requests}_requests_poisson_50_per_s", "requests": args.requests,
+                   "large_jobs": rec["large_jobs"], "frames": rec["frames"], "mode": "fft"},
+        "serve": rec,
     }
     print(json.dumps(line))
 
@@ -805,6 +833,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the accuracy check and the f64/other-mode runs")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving record of the default line")
     ap.add_argument("--validate", action="store_true", help="report sampled errors against exact FP64 spectra")
     ap.add_argument("--requests", type=int, default=100, help="serve: number of requests")
     args = ap.parse_args()

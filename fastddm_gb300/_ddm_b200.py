@@ -128,6 +128,9 @@ class DdmPlan:
     has_window: bool
     precision: str = "ff"
     device: Optional["torch.device"] = None
+    # a caller-owned device buffer to use as the workspace (e.g. a slice of a
+    # preallocated pool); None: the plan allocates its own
+    workspace: Optional["torch.Tensor"] = None
 
     def __post_init__(self):
         _require_torch()
@@ -148,6 +151,10 @@ class DdmPlan:
                 )
             )
             self.workspace_bytes = int(size.value)
+            if self.workspace is not None:
+                if self.workspace.numel() * self.workspace.element_size() < self.workspace_bytes:
+                    raise ValueError(f"workspace too small: {self.workspace_bytes} bytes needed")
+                return
             out_bytes = (len(self._lags_c) + 2) * self.ny * (self.nx // 2 + 1) * 8
             free, _ = torch.cuda.mem_get_info(self.device)
             cached = torch.cuda.memory_reserved(self.device) - torch.cuda.memory_allocated(self.device)

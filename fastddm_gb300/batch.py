@@ -67,10 +67,13 @@ class BatchPlan:
     up the temporal stages (``fddm_b200_batch_create``); :meth:`run` enqueues
     the batch's kernels only (``fddm_b200_batch_launch``).  With
     ``graph=True`` the first run also captures that launch into a CUDA graph
-    and every later run replays the graph.
+    and every later run replays the graph.  `workspace` is an optional
+    caller-owned device buffer of at least ``fddm_b200_batch_workspace_size``
+    bytes.
     """
 
-    def __init__(self, jobs: List[BatchJob], precision: str = "ff", device=None, graph: bool = False):
+    def __init__(self, jobs: List[BatchJob], precision: str = "ff", device=None, graph: bool = False,
+                 workspace: Optional["torch.Tensor"] = None):
         if torch is None or not torch.cuda.is_available():
             raise RuntimeError("the b200 batch needs a CUDA device (GB300)")
         self.device = device or torch.device("cuda", torch.cuda.current_device())
@@ -100,11 +103,16 @@ class BatchPlan:
         with torch.cuda.device(self.device):
             _lib.check(lib.fddm_b200_batch_workspace_size(self._table, len(jobs), _lib.PREC[precision], ctypes.byref(size)))
             self.workspace_bytes = int(size.value)
-            free, _ = torch.cuda.mem_get_info(self.device)
-            cached = torch.cuda.memory_reserved(self.device) - torch.cuda.memory_allocated(self.device)
-            if self.workspace_bytes > 0.9 * (free + cached):
-                raise RuntimeError("Not enough memory")
-            self.workspace = torch.empty(max(1, self.workspace_bytes), dtype=torch.uint8, device=self.device)
+            if workspace is not None:  # caller-owned (e.g. a slice of a preallocated pool)
+                if workspace.numel() * workspace.element_size() < self.workspace_bytes:
+                    raise ValueError(f"workspace too small: {self.workspace_bytes} bytes needed")
+                self.workspace = workspace
+            else:
+                free, _ = torch.cuda.mem_get_info(self.device)
+                cached = torch.cuda.memory_reserved(self.device) - torch.cuda.memory_allocated(self.device)
+                if self.workspace_bytes > 0.9 * (free + cached):
+                    raise RuntimeError("Not enough memory")
+                self.workspace = torch.empty(max(1, self.workspace_bytes), dtype=torch.uint8, device=self.device)
             handle = ctypes.c_void_p()
             self._stream = torch.cuda.current_stream(self.device)
             _lib.check(lib.fddm_b200_batch_create(self._table, len(jobs), _lib.PREC[precision],

@@ -446,41 +446,49 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     } else if (autotune_enabled()) {
       // time every candidate on this call's spectrum (the real launch below
       // rewrites these outputs); another candidate replaces the model's choice
-      // only when it is at least 3 % faster, so timing noise keeps the model
+      // only when it is at least 5 % faster, so timing noise keeps the model
       cudaEvent_t e0, e1;
       if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
         // the same modes for every candidate: several waves of the largest grid
         const size_t probe = std::min<size_t>(Q, 4 * (size_t)(long_fft ? kMaxLongCtas : kMaxTemporalCtas));
-        float best = 1e30f, model_ms = 1e30f;
-        TemporalChoice fastest = model;
-        bool ok = true;
-        for (const TemporalChoice& c : cands) {
-          const int o = occupancy(kernel, c);
+        // three interleaved rounds over the candidates (drift of the clock or
+        // of other work on the GPU hits every candidate alike); fastest of each
+        std::vector<float> tbest(cands.size(), 1e30f);
+        std::vector<unsigned> grids(cands.size(), 0);
+        for (size_t i = 0; i < cands.size(); ++i) {
+          const int o = occupancy(kernel, cands[i]);
           if (o < 1) continue;
           const size_t g = std::min<size_t>((size_t)o * nsm, long_fft ? kMaxLongCtas : kMaxTemporalCtas);
-          const unsigned grid = (unsigned)std::min(g, probe);
-          float ms = 1e30f;
-          launch_range(kernel, c, 0, probe, grid);  // warm-up
-          for (int rep = 0; rep < 3 && ok; ++rep) {  // the fastest of three timed launches
+          grids[i] = (unsigned)std::min(g, probe);
+          launch_range(kernel, cands[i], 0, probe, grids[i]);  // warm-up
+          count_launches(1);
+        }
+        bool ok = true;
+        for (int round = 0; round < 3 && ok; ++round)
+          for (size_t i = 0; i < cands.size() && ok; ++i) {
+            if (!grids[i]) continue;
             float m = 0.0f;
             cudaEventRecord(e0, st);
-            launch_range(kernel, c, 0, probe, grid);
+            launch_range(kernel, cands[i], 0, probe, grids[i]);
             cudaEventRecord(e1, st);
             ok = cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&m, e0, e1) == cudaSuccess;
-            if (ok) ms = std::min(ms, m);
+            if (ok) tbest[i] = std::min(tbest[i], m);
+            count_launches(1);
           }
-          count_launches(4);
-          if (!ok) break;
-          if (c.threads == model.threads && c.need_in_smem == model.need_in_smem) model_ms = ms;
-          if (ms < best) {
-            best = ms;
-            fastest = c;
+        float best = 1e30f, model_ms = 1e30f;
+        TemporalChoice fastest = model;
+        for (size_t i = 0; i < cands.size(); ++i) {
+          if (!grids[i]) continue;
+          if (cands[i].threads == model.threads && cands[i].need_in_smem == model.need_in_smem) model_ms = tbest[i];
+          if (tbest[i] < best) {
+            best = tbest[i];
+            fastest = cands[i];
           }
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (ok) {
-          pick = best < 0.97f * model_ms ? fastest : model;
+          pick = best < 0.95f * model_ms ? fastest : model;
           record_temporal(tune_prec, r.mode, T, nl, pick);
         }
       }

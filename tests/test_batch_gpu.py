@@ -86,13 +86,15 @@ def test_served_results_identical_alone_and_in_the_mix(fddm):
     stacks = _stacks()
     frames = [torch.from_numpy(s.astype(np.int32)).to(dev).to(torch.int16) for s in stacks]
     lags = [np.arange(1, s.shape[0]) for s in stacks]
-    ex = GpuExecutor(0, "ff", n_streams=4)
-    server = DdmServer(ex, memory_budget=8 << 30)
+    ex = GpuExecutor(0, "ff", n_streams=4, pool_bytes=2 << 30)
+    server = DdmServer(ex, memory_budget=8 << 30, small_bytes=16 << 20)
     ex.clock_start()
     reqs = [Request(i, frames[i], lags[i], "fft", None, arrival=0.0) for i in range(len(stacks))]
     done = replay(server, reqs, time.perf_counter)
     assert sorted(r.rid for r in done) == list(range(len(stacks)))
     assert server.peak_inflight >= 2  # requests overlapped on the device
+    assert server.batches >= 1  # small requests admitted together ran as one batch
+    assert ex.pool.available == ex.pool.size  # every pooled workspace returned
     for i, s in enumerate(stacks):
         alone = fddm.ddm(s, lags[i], mode="fft")
         np.testing.assert_array_equal(server.fetch(i).cpu().numpy(), alone._data)
