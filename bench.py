@@ -209,6 +209,50 @@ def time_tier(DdmPlan, mode, T, H, W, code, lags, nx, ny, nt, window, precision,
             "steps": steps}
 
 
+def azavg_record(out, nx: int, ny: int, device, bins: int = 512, reps: int = 3) -> dict:
+    """The azimuthal average of the timed result (``bins`` bins over (0, ky[-1])), both kernel orders.
+
+    Times the host set-up (bin search, weights, per-bin sums) and the device
+    call (set-up tables to the device, one kernel, results left on the device)
+    with CUDA events, best of `reps`; reports the largest relative difference of
+    the fast order against the bit-exact one.
+    """
+    import torch
+
+    from fastddm_gb300 import azimuthalaverage as aa
+
+    kx = 2 * np.pi * np.fft.fftfreq(nx)[: nx // 2 + 1]
+    ky = 2 * np.pi * np.fft.fftshift(np.fft.fftfreq(ny))
+    counts = np.full((ny, nx // 2 + 1), 2)
+    counts[:, 0] = 1
+    counts[:, -1] = 1 if nx % 2 == 0 else 2
+    gx, gy = np.meshgrid(kx, ky)
+    t0 = time.perf_counter()
+    setup = aa.bin_setup(np.sqrt(gx ** 2 + gy ** 2), bins, (0, ky[-1]), None, None, counts, True)
+    host_ms = 1000 * (time.perf_counter() - t0)
+    rec = {"bins": bins, "pixels": int(ny * (nx // 2 + 1)), "rows": int(out.shape[0]), "host_setup_ms": host_ms}
+    res = {}
+    stream = torch.cuda.current_stream(device)
+    for label, exact in (("exact", True), ("fast", False)):
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            avg, err = aa._run_device(out, setup, True, device, exact, host=False)
+            e1.record(stream)
+            torch.cuda.synchronize(device)
+            best = min(best, e0.elapsed_time(e1))
+        rec[f"{label}_ms"] = best
+        res[label] = (avg, err)
+    diff = 0.0
+    for i in range(2):
+        a, b = res["fast"][i], res["exact"][i]
+        ok = ~torch.isnan(b)
+        diff = max(diff, float(((a[ok] - b[ok]).abs() / b[ok].abs().clamp_min(1e-300)).max()))
+    rec["fast_vs_exact_max_rel"] = diff
+    return rec
+
+
 # ---------------------------------------------------------------------------
 # clocks
 # ---------------------------------------------------------------------------
@@ -481,6 +525,11 @@ def run_ours(args):
                      "job_frac": (t_inst + s_inst) / (ms_step / 1000.0) / cyc / 4.0,
                      "sm_mhz": mhz, "source": ic["source"]}
 
+    # the azimuthal average of the timed result (512 bins), both kernel orders
+    azavg = None
+    if rank == 0 and not args.no_check:
+        azavg = azavg_record(out, nx, ny, device)
+
     # end to end through the public API: pinned host frames in, host result out
     e2e = None
     if not args.no_e2e and rank == 0:
@@ -572,6 +621,7 @@ def run_ours(args):
             "roofline": roofline, "issue_roofline": issue, "cpu_baseline": cpu, "e2e": e2e,
             "e2e_pageable": e2e_pageable, "accuracy": accuracy,
             "max_rel_err": accuracy["max_rel_err"] if accuracy else None, "f64_path": f64, "serve": serve,
+            "azimuthal_average": azavg,
             "clocks": clocks, "gpu_launches": launches,
         }
         print(json.dumps(line))
@@ -755,7 +805,7 @@ def serve_records(args, n_req: int, device) -> dict:
         torch.cuda.empty_cache()
         free, _ = torch.cuda.mem_get_info(device)
         ex = GpuExecutor(0, prec, streams, pool_bytes=int(0.35 * free))
-        server = DdmServer(ex, int(0.85 * free), small_bytes=64 << 20) if streams > 1 else \
+        server = DdmServer(ex, int(0.85 * free), small_bytes=512 << 20) if streams > 1 else \
             DdmServer(ex, int(0.85 * free), small_bytes=0)
         # warm-up: FFT tables of every frame size and every temporal length in the stream
         for side in sorted({sc.height for sc in scenes}):

@@ -117,6 +117,10 @@ _SIGNATURES = {
         ctypes.c_int,
         [_vp, _u64, _u64, _vp, _vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp],
     ),
+    "fddm_b200_azimuthal_average_fast": (
+        ctypes.c_int,
+        [_vp, _u64, _u64, _vp, _vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp],
+    ),
     "fddm_b200_polyfit_noise": (
         ctypes.c_int, [_vp, _u64, _u64, _vp, _vp, _u64, ctypes.c_double, _vp, _vp, _vp]
     ),

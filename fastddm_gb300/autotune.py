@@ -78,12 +78,12 @@ def save_table(path: Path = TABLE_PATH, device: str = "") -> None:
     Path(path).write_text(json.dumps({"device": device, "entries": rows}, indent=1) + "\n")
 
 
-def tune_classes(classes: Iterable[Tuple[str, str, int, int]], side: int = 192, gpu_id: int = 0) -> List[dict]:
-    """Time every candidate launch shape for each (precision, mode, frames, nlags) class.
+def tune_classes(classes: Iterable[Tuple], side: int = 192, gpu_id: int = 0) -> List[dict]:
+    """Time every candidate launch shape for each (precision, mode, frames, nlags[, side]) class.
 
-    Each class runs once on a synthetic stack of `side` x `side` frames with
-    the autotuner on (a class already in the table is skipped); returns the
-    table afterwards.
+    Each class runs once on a synthetic stack of side x side frames (`side`
+    unless the class names its own) with the autotuner on (a class already in
+    the table is skipped); returns the table afterwards.
     """
     import numpy as np
     import torch
@@ -94,16 +94,18 @@ def tune_classes(classes: Iterable[Tuple[str, str, int, int]], side: int = 192, 
     device = torch.device("cuda", gpu_id)
     enable(True)
     try:
-        for precision, mode, T, nl in classes:
+        for cls in classes:
+            precision, mode, T, nl = cls[:4]
+            sd = cls[4] if len(cls) > 4 else side
             if lookup(precision, mode, T, nl) is not None:
                 continue
             lags = np.unique(np.round(np.geomspace(1, T - 1, nl)).astype(int)) if nl < T - 1 else np.arange(1, T)
             if len(lags) != nl:  # geometric spacing collided: fill with the smallest unused lags
                 extra = np.setdiff1d(np.arange(1, T), lags)[: nl - len(lags)]
                 lags = np.sort(np.concatenate([lags, extra]))
-            frames = torch.randint(0, 255, (T, side, side), dtype=torch.uint8, device=device)
+            frames = torch.randint(0, 255, (T, sd, sd), dtype=torch.uint8, device=device)
             nt = next_fast_len(2 * T, "b200") if mode == "fft" else 0
-            plan = DdmPlan(mode, T, side, side, 0, lags, side, side, nt, False, precision, device)
+            plan = DdmPlan(mode, T, sd, sd, 0, lags, sd, sd, nt, False, precision, device)
             out = torch.empty(plan.out_shape, dtype=torch.float64, device=device)
             plan.run(frames, None, out)
             torch.cuda.synchronize(device)
@@ -123,13 +125,14 @@ if __name__ == "__main__":  # pragma: no cover - run on a GB300 to refresh the c
     args = ap.parse_args()
     from . import synthetic
 
-    classes = [("ff", "fft", 4000, 200), ("ff", "fft", 512, 511), ("ff", "fft", 64, 63), ("ff", "fft", 20000, 200),
-               ("ff", "diff", 4000, 200), ("ff", "diff", 512, 511), ("f64", "fft", 4000, 200),
-               ("f32", "fft", 4000, 200)]
+    # the benchmark workloads at their own frame sizes
+    classes = [("ff", "fft", 4000, 200, 1024), ("ff", "fft", 512, 511, 512), ("ff", "fft", 64, 63, 128),
+               ("ff", "fft", 20000, 200, 256), ("ff", "diff", 4000, 200, 1024), ("ff", "diff", 512, 511, 512),
+               ("f64", "fft", 4000, 200, 1024), ("f32", "fft", 4000, 200, 1024)]
     # the uneven-stack batch: every length of the seeded 96-stack draw, all lags
     for sc in synthetic.config4_scenes(96, seed=0):
         classes.append(("ff", "fft", sc.length, sc.length - 1))
-    classes = list(dict.fromkeys(classes))
+    classes = list(dict.fromkeys(classes))  # first occurrence of a class wins
     load_table(Path(args.out))
     tune_classes(classes)
     import torch

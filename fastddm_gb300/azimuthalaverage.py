@@ -170,7 +170,8 @@ def _device_of(gpu_id):
     return torch.device("cuda", int(gpu_id))
 
 
-def _run_device(data_dev, setup: BinSetup, eval_err: bool, device) -> Tuple[np.ndarray, Optional[np.ndarray]]:
+def _run_device(data_dev, setup: BinSetup, eval_err: bool, device, exact: bool = True,
+                host: bool = True):
     nrows = int(data_dev.shape[0])
     npix = int(np.prod(data_dev.shape[1:]))
     n_bins = setup.n_bins
@@ -194,13 +195,16 @@ def _run_device(data_dev, setup: BinSetup, eval_err: bool, device) -> Tuple[np.n
     err = torch.empty((n_bins, nrows), dtype=torch.float64, device=device) if eval_err else None
     lib = _lib.load()
     data_dev = data_dev.contiguous()
+    fn = lib.fddm_b200_azimuthal_average if exact else lib.fddm_b200_azimuthal_average_fast
     with torch.cuda.device(device):
-        code = lib.fddm_b200_azimuthal_average(
+        code = fn(
             data_dev.data_ptr(), nrows, npix, d_off.data_ptr(), d_pix.data_ptr(), n_bins, d_w.data_ptr(),
             d_sw.data_ptr(), d_bias.data_ptr() if d_bias is not None else None, avg.data_ptr(),
             err.data_ptr() if err is not None else None, torch.cuda.current_stream(device).cuda_stream,
         )
     _lib.check(code)
+    if not host:
+        return avg, err
     return avg.cpu().numpy(), (err.cpu().numpy() if err is not None else None)
 
 
@@ -215,12 +219,15 @@ def azimuthal_average_array(
     eval_err: Optional[bool] = True,
     *,
     gpu_id: int = 0,
+    exact: bool = True,
 ) -> Tuple[np.ndarray, ...]:
     """Weighted azimuthal average of a 3D array (numpy, or a CUDA tensor already on the device).
 
     Returns ``(avg, err, k, bin_edges)``; ``avg``/``err`` have shape
     ``(n_bins, len(data))``, empty bins are NaN, ``err`` is None when
-    ``eval_err`` is False.
+    ``eval_err`` is False.  ``exact=True`` reproduces the reference's per-pixel
+    loops bit for bit; ``exact=False`` sums each bin with a warp of fused
+    multiply-adds (rounding-level differences, much faster on large maps).
     """
     dim_y, dim_x = tuple(data.shape[-2:])
     if dist.shape != (dim_y, dim_x):
@@ -231,7 +238,7 @@ def azimuthal_average_array(
         data_dev = data.to(device=device, dtype=torch.float64)
     else:
         data_dev = torch.from_numpy(np.ascontiguousarray(data, dtype=np.float64)).to(device)
-    avg, err = _run_device(data_dev, setup, bool(eval_err), device)
+    avg, err = _run_device(data_dev, setup, bool(eval_err), device, exact)
     return avg, err, setup.k, setup.bin_edges
 
 
@@ -244,8 +251,11 @@ def azimuthal_average(
     eval_err: Optional[bool] = True,
     *,
     gpu_id: int = 0,
+    exact: bool = True,
 ) -> AzimuthalAverage:
     """Azimuthal average of an image structure function (reference ``:481-564``).
+
+    ``exact`` as in :func:`azimuthal_average_array`.
 
     Column 0 counts once, the last column once when the full width is even,
     every other column twice (its mirror image in the full plane).
@@ -257,6 +267,6 @@ def azimuthal_average(
     k_modulus = np.sqrt(gx ** 2 + gy ** 2)
     data = img_str_func._device_data if img_str_func._device_data is not None else img_str_func._data
     avg, err, k, edges = azimuthal_average_array(
-        data, k_modulus, bins, range, mask, weights, counts, eval_err, gpu_id=gpu_id
+        data, k_modulus, bins, range, mask, weights, counts, eval_err, gpu_id=gpu_id, exact=exact
     )
     return AzimuthalAverage(avg, err, k, img_str_func.tau, edges)
