@@ -31,7 +31,11 @@ def bound_reference(monkeypatch):
     sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
     import make_golden
 
-    before = dict(sys.modules)  # the import stubs out file readers; everything is put back afterwards
+    # the reference package ("fastddm") and the stand-ins it gets for file readers are removed afterwards
+    def ours(k):
+        return k == "fastddm" or k.startswith("fastddm.") or k in ("tifffile", "skimage", "skimage.io", "nd2reader")
+
+    before = {k: v for k, v in sys.modules.items() if ours(k)}
     mods = make_golden.import_reference(REF)
     ref_ddm, ref_fftopt = mods["_ddm"], mods["_fftopt"]
 
@@ -71,7 +75,7 @@ def bound_reference(monkeypatch):
 
     monkeypatch.setattr(_ddm_b200, "ddm_device", fake_device)
     yield ref_ddm, calls
-    for k in [k for k in sys.modules if k not in before]:
+    for k in [k for k in sys.modules if ours(k)]:
         del sys.modules[k]
     sys.modules.update(before)
 
