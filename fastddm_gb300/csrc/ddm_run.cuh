@@ -449,8 +449,9 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
       // only when it is at least 5 % faster, so timing noise keeps the model
       cudaEvent_t e0, e1;
       if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
-        // the same modes for every candidate: several waves of the largest grid
-        const size_t probe = std::min<size_t>(Q, 4 * (size_t)(long_fft ? kMaxLongCtas : kMaxTemporalCtas));
+        // the same modes for every candidate: 16 waves of the largest grid, so
+        // that per-CTA set-up is amortised as in a full launch
+        const size_t probe = std::min<size_t>(Q, 16 * (size_t)(long_fft ? kMaxLongCtas : kMaxTemporalCtas));
         // three interleaved rounds over the candidates (drift of the clock or
         // of other work on the GPU hits every candidate alike); fastest of each
         std::vector<float> tbest(cands.size(), 1e30f);
