@@ -394,10 +394,16 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
     return shared_fft ? temporal_fft_smem(T, N, nl, sizeof(cx<S>), sizeof(A), nis != 0) : smem_t;
   };
   std::vector<TemporalChoice> cands;
+  // diff mode with the series read through L1/L2 (too long for shared memory):
+  // all warps of a CTA read one mode's series for their lags, so only the
+  // largest CTA keeps that series in L1 (with 128-thread CTAs, 16 modes per SM
+  // thrash it: 20000 x 256^2, 200 lags, temporal 449 ms against 271)
+  const bool diff_global = r.mode == MODE_DIFF && !L.diff_staged;
   for (int nis : {1, 0}) {
     // the tables' placement only matters to the shared-memory fft kernel
     if (shared_fft ? (nis == 1 && with_need > kSmemLimit) : nis == 1) continue;
-    for (int t : {512, 256, 128}) cands.push_back({t, nis});
+    for (int t : {512, 256, 128})
+      if (!diff_global || t == 512) cands.push_back({t, nis});
   }
   auto occupancy = [&](auto kernel, const TemporalChoice& c) {
     int o = 0;
