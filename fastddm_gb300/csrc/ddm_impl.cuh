@@ -223,7 +223,7 @@ template <class S> __global__ void k_window_convert(const double* __restrict__ w
 // frame) of one frame chunk.  When rows are 16-byte aligned the raw pixels of
 // the next item are copied with cp.async into a double-buffered staging area
 // while the current item is transformed.
-// dynamic smem: swz_round(pairs * nx) * cx<S> [+ 2 * raw_stage_bytes]
+// dynamic smem: swz_round(pairs * (nx + G)) * cx<S> [+ 2 * raw_stage_bytes] + nx ints
 // ---------------------------------------------------------------------------
 template <class S, class IN>
 __device__ __forceinline__ void rows_issue_raw(const SpatialArgs& a, int item, unsigned char* raw, int ngroups,
@@ -261,6 +261,10 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
   const bool u8_fast = sizeof(IN) == 1 && async_raw && !win && W == nx && lgnx >= 2;
   unsigned char* raw[2] = {smem_raw + (size_t)swz_round<S>(a.pairs_per_block * ld) * sizeof(cx<S>), nullptr};
   raw[1] = raw[0] + a.raw_stage_bytes;
+  // the digit-reversal permutation of the row transform, read by every unpack
+  // (made visible by the first item's barrier)
+  int* perm = reinterpret_cast<int*>(raw[1] + a.raw_stage_bytes);
+  for (int i = tid; i < nx; i += nthr) perm[i] = a.permx[i];
   int b = 0;
   if (async_raw && (int)blockIdx.x < nitems) rows_issue_raw<S, IN>(a, blockIdx.x, raw[0], ngroups, tid, nthr);
 
@@ -325,8 +329,8 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
     for (int e = tid; e < np * nkx; e += nthr) {
       const int k = lgp >= 0 ? e >> lgp : e / np;
       const int p = e - k * np;
-      const cx<S> zk = buf[swz<S>(p * ld + a.permx[k])];
-      const cx<S> zn = buf[swz<S>(p * ld + a.permx[k == 0 ? 0 : nx - k])];
+      const cx<S> zk = buf[swz<S>(p * ld + perm[k])];
+      const cx<S> zn = buf[swz<S>(p * ld + perm[k == 0 ? 0 : nx - k])];
       cx<S>* dst = R + (size_t)k * a.Hpad + 2 * (pair0 + p);
       dst[0] = {sc<S>::half(sc<S>::add(zk.r, zn.r)), sc<S>::half(sc<S>::sub(zk.i, zn.i))};
       dst[1] = {sc<S>::half(sc<S>::add(zk.i, zn.i)), sc<S>::half(sc<S>::sub(zn.r, zk.r))};
@@ -340,7 +344,7 @@ __global__ void __launch_bounds__(256) k_rows(SpatialArgs a) {
 // group of frames) of one frame chunk; the next item's columns are copied with
 // cp.async into the second of two transform buffers while the current item
 // is transformed.
-// dynamic smem: 2 * swz_round(cols * frames * ny) * cx<S>
+// dynamic smem: 2 * swz_round(cols * frames * (ny + G)) * cx<S> + ny ints
 // ---------------------------------------------------------------------------
 template <class S>
 __device__ __forceinline__ void cols_issue(const SpatialArgs& a, int item, cx<S>* buf, int ncg, int ld, int tid,
@@ -367,9 +371,9 @@ __device__ __forceinline__ void cols_issue(const SpatialArgs& a, int item, cx<S>
 // Store phase of the column pass: scale by 1/sqrt(nx ny), apply the y-fftshift and
 // write F[q][t].  P2: the scale is a power of two and one multiply per word is exact.
 template <class S, bool P2>
-__device__ __forceinline__ void cols_store(const SpatialArgs& a, const cx<S>* buf, cx<S>* F, int ld, int kc0,
-                                           int tl0, int nk, int ntg, int lgTG, int lgCK, S norm, int tid,
-                                           int nthr) {
+__device__ __forceinline__ void cols_store(const SpatialArgs& a, const cx<S>* buf, const int* __restrict__ perm,
+                                           cx<S>* F, int ld, int kc0, int tl0, int nk, int ntg, int lgTG, int lgCK,
+                                           S norm, int tid, int nthr) {
   const int ny = a.ny, nkx = a.nkx, CK = a.cols_per_block, TG = a.frames_per_block;
   const int half = ny >> 1;
   for (int e = tid; e < CK * TG * ny; e += nthr) {
@@ -377,7 +381,7 @@ __device__ __forceinline__ void cols_store(const SpatialArgs& a, const cx<S>* bu
     if (lgTG >= 0) { tl = e & (TG - 1); rest = e >> lgTG; } else { tl = e % TG; rest = e / TG; }
     if (lgCK >= 0) { kc = rest & (CK - 1); ky = rest >> lgCK; } else { kc = rest % CK; ky = rest / CK; }
     if (tl < ntg && kc < nk) {
-      const cx<S> z = buf[swz<S>((tl * CK + kc) * ld + a.permy[ky])];
+      const cx<S> z = buf[swz<S>((tl * CK + kc) * ld + perm[ky])];
       cx<S> v;
       if constexpr (P2) {
         v = {sc<S>::mul_p2(z.r, a.norm_h), sc<S>::mul_p2(z.i, a.norm_h)};
@@ -408,6 +412,10 @@ __global__ void __launch_bounds__(512) k_cols(SpatialArgs a) {
   // 1/sqrt(nx ny) is a power of two when nx ny is a power of four: exact scaling
   const bool norm_p2 = a.norm_l == 0.0f && (__float_as_uint(a.norm_h) & 0x007FFFFFu) == 0u;
   cx<S>* F = reinterpret_cast<cx<S>*>(a.spec);
+  // the digit-reversal permutation of the column transform, read by every store
+  // (made visible by the first item's barrier)
+  int* perm = reinterpret_cast<int*>(bufs[1] + swz_round<S>(NB * ld));
+  for (int i = tid; i < ny; i += nthr) perm[i] = a.permy[i];
   int b = 0;
   if ((int)blockIdx.x < nitems) cols_issue<S>(a, blockIdx.x, bufs[0], ncg, ld, tid, nthr);
 
@@ -421,9 +429,9 @@ __global__ void __launch_bounds__(512) k_cols(SpatialArgs a) {
     const int nk = min(CK, nkx - kc0), ntg = min(TG, a.tc - tl0);
     fft_forward<S, P2>(buf, NB, ld, a.py, reinterpret_cast<const cx<S>*>(a.twy), tid, nthr);
     if (norm_p2)
-      cols_store<S, true>(a, buf, F, ld, kc0, tl0, nk, ntg, lgTG, lgCK, norm, tid, nthr);
+      cols_store<S, true>(a, buf, perm, F, ld, kc0, tl0, nk, ntg, lgTG, lgCK, norm, tid, nthr);
     else
-      cols_store<S, false>(a, buf, F, ld, kc0, tl0, nk, ntg, lgTG, lgCK, norm, tid, nthr);
+      cols_store<S, false>(a, buf, perm, F, ld, kc0, tl0, nk, ntg, lgTG, lgCK, norm, tid, nthr);
     b ^= 1;
   }
 }

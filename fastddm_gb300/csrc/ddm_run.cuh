@@ -272,8 +272,10 @@ int run_ddm_t(const DdmRequest& r, cudaStream_t st, std::string& err) {
   // raw rows staged asynchronously when every row starts on a 16-byte boundary
   sa.raw_stage_bytes = stageable(sa.img) ? (int)stage : 0;
   const int G = swz_group<S>::G;
-  const size_t smem_rows = (size_t)swz_round<S>(L.pairs_per_block * (nx + G)) * sizeof(cx<S>) + 2 * (size_t)sa.raw_stage_bytes;
-  const size_t smem_cols = 2 * (size_t)swz_round<S>(L.cols_per_block * L.frames_per_block * (ny + G)) * sizeof(cx<S>);
+  const size_t smem_rows = (size_t)swz_round<S>(L.pairs_per_block * (nx + G)) * sizeof(cx<S>) +
+                           2 * (size_t)sa.raw_stage_bytes + (size_t)nx * sizeof(int);
+  const size_t smem_cols =
+      2 * (size_t)swz_round<S>(L.cols_per_block * L.frames_per_block * (ny + G)) * sizeof(cx<S>) + (size_t)ny * sizeof(int);
   const int ngroups = (npairs + L.pairs_per_block - 1) / L.pairs_per_block;
   const bool p2y = plan_is_p2(sa.py);
   if ((ce = p2y ? allow_smem(k_cols<S, true>, smem_cols) : allow_smem(k_cols<S, false>, smem_cols)) != cudaSuccess) {

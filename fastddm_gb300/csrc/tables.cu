@@ -418,14 +418,15 @@ bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err) {
   const int nb = (int)std::max<size_t>(1, cols_target / ((size_t)r.ny * es));
   L.frames_per_block = std::min(nb, env_int("FDDM_B200_COLS_FRAMES", 8));
   L.cols_per_block = std::max(1, nb / L.frames_per_block);
+  // two transform buffers and the permutation table (ny ints)
   auto cols_bytes = [&] {
-    return (size_t)(2 * (L.frames_per_block * L.cols_per_block * (r.ny + g) + g)) * es;
+    return (size_t)(2 * (L.frames_per_block * L.cols_per_block * (r.ny + g) + g)) * es + (size_t)r.ny * 4;
   };
   while (cols_bytes() > kSmemLimit && L.cols_per_block > 1) L.cols_per_block /= 2;
   while (cols_bytes() > kSmemLimit && L.frames_per_block > 1) L.frames_per_block /= 2;
   // row pass: one transform buffer + at most 64 KB of raw staging; column pass: two buffers
-  if ((size_t)(L.pairs_per_block * (r.nx + g) + g) * es + 65536 > kSmemLimit ||
-      (size_t)(2 * (L.frames_per_block * L.cols_per_block * (r.ny + g) + g)) * es > kSmemLimit) {
+  if ((size_t)(L.pairs_per_block * (r.nx + g) + g) * es + 65536 + (size_t)r.nx * 4 > kSmemLimit ||
+      cols_bytes() > kSmemLimit) {
     err = "image dimensions too large for the shared-memory FFT";
     return false;
   }
