@@ -41,6 +41,7 @@ CONFIGS = {
     "long": "CONFIG_LONG",     # 20000 x 256^2 uint8, 200 log lags (split temporal transform)
     "batch": None,             # 96 uneven stacks in one batch call (run_batch)
     "serve": None,             # Poisson request stream through the serving loop (run_serve)
+    "dft_stage": None,         # the tensor-core DFT-stage decision measurement (run_dft_stage)
 }
 
 
@@ -871,6 +872,43 @@ def run_serve(args):
     print(json.dumps(line))
 
 
+def run_dft_stage(args):
+    """The first radix-32 stage of the row transform of 1024-pixel 8-bit rows, two ways: the two
+    float-float butterfly passes, and the CUDA-core work a 5-slice bf16 DFT-as-GEMM stage would still
+    need (slice-sum combination, row packing, twiddle; no MMA: a lower bound on its time)."""
+    import torch
+
+    from fastddm_gb300 import _build, _lib
+
+    _build.build()
+    lib = _lib.load()
+    device = torch.device("cuda", 0)
+    npairs = 32768  # 64 frames of 1024 x 1024
+    g = torch.Generator(device=device)
+    g.manual_seed(0)
+    rows = torch.randint(0, 256, (npairs * 2 * 1024,), dtype=torch.uint8, device=device, generator=g)
+    out = torch.empty((npairs * 1024 * 16,), dtype=torch.uint8, device=device)
+    stream = torch.cuda.current_stream(device)
+    res = {}
+    for variant, label in ((0, "float_float_butterflies"), (1, "tensor_stage_cuda_core_floor")):
+        for _ in range(args.warmup):
+            _lib.check(lib.fddm_b200_experiment_dft_stage(variant, rows.data_ptr(), npairs, out.data_ptr(),
+                                                          stream.cuda_stream))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            _lib.check(lib.fddm_b200_experiment_dft_stage(variant, rows.data_ptr(), npairs, out.data_ptr(),
+                                                          stream.cuda_stream))
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        ms = e0.elapsed_time(e1) / args.steps
+        res[label] = {"ms_per_launch": ms, "us_per_frame": 1000 * ms / 64}
+    res["floor_over_butterflies"] = res["tensor_stage_cuda_core_floor"]["ms_per_launch"] / \
+        res["float_float_butterflies"]["ms_per_launch"]
+    print(json.dumps({"measurement": "dft_stage", "rows": npairs * 2, "row_length": 1024, "frames": 64,
+                      "steps": args.steps, "results": res}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -893,6 +931,8 @@ def main():
         run_batch(args)
     elif args.config == "serve":
         run_serve(args)
+    elif args.config == "dft_stage":
+        run_dft_stage(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

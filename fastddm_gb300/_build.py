@@ -20,7 +20,7 @@ BUILD_DIR = PKG_DIR / "_build"
 LIB_NAME = "libfddm_b200.so"
 LIB_PATH = PKG_DIR / LIB_NAME
 
-SOURCES = ["capi.cu", "tables.cu", "tune.cu", "azavg.cu", "noalloc.cu", "batch.cu", "sfio.cu", "tiffio.cpp", "postproc.cu", "ddm_ff.cu", "ddm_f64.cu",
+SOURCES = ["capi.cu", "tables.cu", "tune.cu", "azavg.cu", "noalloc.cu", "batch.cu", "sfio.cu", "tiffio.cpp", "postproc.cu", "dftstage.cu", "ddm_ff.cu", "ddm_f64.cu",
            "ddm_f32.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC)]

@@ -101,6 +101,7 @@ _SIGNATURES = {
     "fddm_b200_stage_times": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "fddm_b200_launch_count": (ctypes.c_uint64, []),
     "fddm_b200_last_input_path": (ctypes.c_int, []),
+    "fddm_b200_experiment_dft_stage": (ctypes.c_int, [ctypes.c_int, _vp, _u64, _vp, _vp]),
     "fddm_b200_set_autotune": (ctypes.c_int, [ctypes.c_int]),
     "fddm_b200_tuning_set": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _u64, _u64, ctypes.c_int, ctypes.c_int]),
     "fddm_b200_tuning_get": (

@@ -211,6 +211,8 @@ size_t spec_elem_bytes(int precision);
 bool plan_layout(const DdmRequest& r, WorkLayout& L, std::string& err);
 // Factor n into supported radices; false if n has another prime factor.
 bool make_plan(int n, FftPlan& p);
+// Plan of length n with the given radices (their product must be n).
+bool plan_from_radices(int n, const int* radices, int npass, FftPlan& p);
 // Plan of length n/2 whose digit-reversed order matches the even outputs of
 // p: radices (R_0/2, R_1, ...), the first dropped when R_0 = 2.  Requires an
 // even n and an even R_0 (make_plan puts the radices 8, 4, 2 first).

@@ -51,6 +51,18 @@ bool make_plan(int n, FftPlan& p) {
   return true;
 }
 
+bool plan_from_radices(int n, const int* radices, int npass, FftPlan& p) {
+  if (npass < 1 || npass > kMaxPass) return false;
+  long long prod = 1;
+  for (int s = 0; s < npass; ++s) prod *= radices[s];
+  if (prod != n) return false;
+  p.n = n;
+  p.npass = npass;
+  for (int s = 0; s < npass; ++s) p.radix[s] = radices[s];
+  finish_plan(p);
+  return true;
+}
+
 bool half_plan(const FftPlan& p, FftPlan& h) {
   if (p.npass < 1 || p.n % 2 || p.radix[0] % 2) return false;
   h.n = p.n / 2;

@@ -316,6 +316,17 @@ int fddm_b200_stage_times(float* spatial_ms, float* temporal_ms);
 uint64_t fddm_b200_launch_count(void);
 int fddm_b200_last_input_path(void);
 
+/* Measurement behind the decision not to run a DFT stage on the tensor cores
+   (no counterpart in the reference).  d_rows holds npairs pairs of 8-bit rows
+   of 1024 pixels; d_out receives npairs x 1024 float-float complex values.
+   variant 0: the two float-float DIF passes (radix 8, radix 4) forming the
+   radix-32 first stage of the packed pair's 1024-point transform, as in the
+   row pass; variant 1: the CUDA-core work a 5-slice bf16 DFT-as-GEMM version
+   of that stage would still need (combining ten FP32 slice sums per output
+   into float-float, packing the pair, the inter-stage twiddle), with the slice
+   sums taken from shared memory and no MMA: a lower bound on its time. */
+int fddm_b200_experiment_dft_stage(int variant, const void* d_rows, uint64_t npairs, void* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
