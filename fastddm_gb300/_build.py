@@ -20,10 +20,14 @@ BUILD_DIR = PKG_DIR / "_build"
 LIB_NAME = "libfddm_b200.so"
 LIB_PATH = PKG_DIR / LIB_NAME
 
-SOURCES = ["capi.cu", "tables.cu", "tune.cu", "azavg.cu", "noalloc.cu", "batch.cu", "sfio.cu", "tiffio.cpp", "postproc.cu", "dftstage.cu", "ddm_ff.cu", "ddm_f64.cu",
-           "ddm_f32.cu"]
+# slowest translation units first, so the parallel build ends sooner
+SOURCES = ["ddm_ff.cu", "ddm_f64.cu", "ddm_f32.cu", "fit_nv7.cu", "fit_nv6.cu", "fit_nv5.cu", "fit_nv4.cu", "fit_nv3.cu",
+           "fit_nv2.cu", "fit_nv1.cu", "batch.cu", "capi.cu", "tables.cu", "tune.cu", "azavg.cu", "noalloc.cu", "sfio.cu",
+           "tiffio.cpp", "postproc.cu", "dftstage.cu", "fit.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC)]
+# per-file flags: the fits follow host arithmetic, which has no multiply-add contraction
+FILE_FLAGS = {f"fit_nv{k}.cu": ["-fmad=false"] for k in range(1, 8)}
 
 
 def _nvcc() -> str:
@@ -55,7 +59,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
 
     def compile_one(src: str) -> tuple[str, str]:
         obj = BUILD_DIR / (Path(src).stem + ".o")
-        cmd = [nvcc, *ARCH, *FLAGS, *extra, "-c", str(CSRC / src), "-o", str(obj)]
+        cmd = [nvcc, *ARCH, *FLAGS, *FILE_FLAGS.get(src, []), *extra, "-c", str(CSRC / src), "-o", str(obj)]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{res.stderr}")

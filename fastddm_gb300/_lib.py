@@ -125,6 +125,13 @@ _SIGNATURES = {
     "fddm_b200_polyfit_noise": (
         ctypes.c_int, [_vp, _u64, _u64, _vp, _vp, _u64, ctypes.c_double, _vp, _vp, _vp]
     ),
+    "fddm_b200_fit_model_nparams": (ctypes.c_int, [ctypes.c_int]),
+    "fddm_b200_fit_workspace_bytes": (ctypes.c_int, [ctypes.c_int, _u64, _u64, ctypes.POINTER(_u64)]),
+    "fddm_b200_fit_lm": (
+        ctypes.c_int,
+        [ctypes.c_int, _u64, _vp, _vp, _u64, _u64, _vp, _u64, _u64, _vp, _u64, _vp, _vp, _u64, ctypes.c_int, _vp,
+         _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u64, _vp],
+    ),
     "fddm_b200_tiff_info": (
         ctypes.c_int,
         [ctypes.c_char_p, ctypes.POINTER(_u64), ctypes.POINTER(_u64), ctypes.POINTER(_u64),

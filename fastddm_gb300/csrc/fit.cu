@@ -1,0 +1,114 @@
+// C ABI of the batched Levenberg-Marquardt fits (device code in fit_lm.cuh;
+// the kernel for each number of varying parameters is compiled in its own
+// translation unit, fit_nv<k>.cu).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <algorithm>
+#include <string>
+#include "fddm_b200.h"
+#include "fddm_internal.h"
+#include "fit_lm.cuh"
+
+namespace {
+
+size_t slot_doubles(uint64_t m, int np) { return (size_t)(2 + np) * m; }
+
+int max_slots() {
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return (nsm > 0 ? nsm : 152) * 8 * fddm::fitlm::kWarpsPerCta;
+}
+
+}  // namespace
+
+using namespace fddm;
+
+extern "C" int fddm_b200_fit_model_nparams(int model) { return fitlm::model_nparams(model); }
+
+extern "C" int fddm_b200_fit_workspace_bytes(int model, uint64_t m, uint64_t nchains, uint64_t* bytes) {
+  set_last_error("");
+  if (!bytes) return fail_with(FDDM_ERR_INVALID, "null pointer argument");
+  const int np = fitlm::model_nparams(model);
+  if (np == 0) return fail_with(FDDM_ERR_INVALID, "unknown fit model");
+  const uint64_t slots = std::min<uint64_t>(nchains, (uint64_t)max_slots());
+  *bytes = (uint64_t)slot_doubles(m, np) * sizeof(double) * slots;
+  return FDDM_OK;
+}
+
+extern "C" int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, const double* d_y, uint64_t ldy,
+                                uint64_t ny, const double* d_w, uint64_t ldw, uint64_t nw,
+                                const int32_t* d_problems, uint64_t nproblems,
+                                const int32_t* d_chain_offsets, const int32_t* d_chain_problems, uint64_t nchains,
+                                int nvary, const double* d_init, const double* d_min, const double* d_max,
+                                const double* options, double* d_values, double* d_stderr, double* d_chisqr,
+                                int32_t* d_nfev, int32_t* d_info, int32_t* d_status, double* d_residual,
+                                void* d_workspace, uint64_t workspace_bytes, void* stream) {
+  set_last_error("");
+  const int np = fitlm::model_nparams(model);
+  if (np == 0) return fail_with(FDDM_ERR_INVALID, "unknown fit model");
+  if (nvary < 1 || nvary > np) return fail_with(FDDM_ERR_INVALID, "nvary must be in 1..nparams");
+  if ((uint64_t)nvary > m) return fail_with(FDDM_ERR_INVALID, "fewer data points than varying parameters");
+  if (m > (1ull << 30) || nproblems > (1ull << 30) || nchains > (1ull << 30) || ny > (1ull << 30) ||
+      nw > (1ull << 30))
+    return fail_with(FDDM_ERR_UNSUPPORTED, "too many data points, problems or chains");
+  if (!options) return fail_with(FDDM_ERR_INVALID, "null options");
+  if (nchains == 0 || nproblems == 0) return FDDM_OK;
+  if (!d_x || !d_y || !d_problems || !d_chain_offsets || !d_chain_problems || !d_init || !d_min || !d_max ||
+      !d_values || !d_stderr || !d_chisqr || !d_nfev || !d_info || !d_status || !d_workspace)
+    return fail_with(FDDM_ERR_INVALID, "null pointer argument");
+  if (ldy < m || (d_w && ldw < m)) return fail_with(FDDM_ERR_INVALID, "row stride shorter than the data");
+  const uint64_t per_slot = (uint64_t)slot_doubles(m, np) * sizeof(double);
+  const uint64_t slots = std::min<uint64_t>({nchains, (uint64_t)max_slots(), workspace_bytes / per_slot});
+  if (slots == 0) return fail_with(FDDM_ERR_NOMEM, "fit workspace smaller than one slot");
+  fitlm::Batch b{};
+  b.model = model;
+  b.np = np;
+  b.m = (int)m;
+  b.x = d_x;
+  b.y = d_y;
+  b.ldy = ldy;
+  b.ny = (int)ny;
+  b.w = d_w;
+  b.ldw = ldw;
+  b.nw = d_w ? (int)nw : 0;
+  b.nprob = (int)nproblems;
+  b.problems = d_problems;
+  b.chain_off = d_chain_offsets;
+  b.chain_list = d_chain_problems;
+  b.nchains = (int)nchains;
+  b.init = d_init;
+  b.lo = d_min;
+  b.hi = d_max;
+  b.ftol = options[0];
+  b.xtol = options[1];
+  b.gtol = options[2];
+  b.epsfcn = options[3];
+  b.factor = options[4];
+  b.max_nfev = options[5] > 0 ? (long long)options[5] : 2000LL * (nvary + 1);
+  b.values = d_values;
+  b.stderr_ = d_stderr;
+  b.chisqr = d_chisqr;
+  b.nfev = d_nfev;
+  b.info = d_info;
+  b.status = d_status;
+  b.residual = d_residual;
+  b.ws = static_cast<double*>(d_workspace);
+  b.slot_doubles = slot_doubles(m, np);
+  b.nslots = (int)slots;
+  const unsigned grid = (unsigned)((slots + fitlm::kWarpsPerCta - 1) / fitlm::kWarpsPerCta);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t ce;
+  switch (nvary) {
+    case 1: ce = fitlm::launch_nv1(b, grid, st); break;
+    case 2: ce = fitlm::launch_nv2(b, grid, st); break;
+    case 3: ce = fitlm::launch_nv3(b, grid, st); break;
+    case 4: ce = fitlm::launch_nv4(b, grid, st); break;
+    case 5: ce = fitlm::launch_nv5(b, grid, st); break;
+    case 6: ce = fitlm::launch_nv6(b, grid, st); break;
+    default: ce = fitlm::launch_nv7(b, grid, st); break;
+  }
+  if (ce != cudaSuccess) return fail_with(FDDM_ERR_CUDA, cudaGetErrorString(ce));
+  count_launches(1);
+  return FDDM_OK;
+}

@@ -1,0 +1,823 @@
+// Batched Levenberg-Marquardt fits of the DDM relaxation models.
+//
+// Replaces the lmfit Model.fit calls of the reference's fit_multik
+// (src/python/fit.py:337, :380) and fit (fit.py:188).
+// lmfit's default method, 'leastsq', runs MINPACK's lmdif through
+// scipy.optimize.leastsq on lmfit's internal (unbounded) parameters.  This file
+// restates that published algorithm (J. J. Moré, "The Levenberg-Marquardt
+// algorithm: implementation and theory", 1978; Moré, Garbow and Hillstrom,
+// MINPACK-1 user guide, 1980) with lmfit's settings: forward-difference
+// Jacobian with step sqrt(max(epsfcn, eps)) |x_j|, Householder QR with column
+// pivoting, Moré's iteration for the Levenberg-Marquardt parameter, the
+// trust-region update, and the ftol / xtol / gtol tests (lmfit passes 1e-7 for
+// all three).  Bounded parameters are mapped as lmfit maps them (the MINUIT
+// transformations): lower only  x = min - 1 + sqrt(u^2 + 1), upper only
+// x = max + 1 - sqrt(u^2 + 1), both  x = min + (sin u + 1)(max - min)/2.
+// The standard errors are lmfit's: the covariance inv(R^T R) of the last
+// factorisation, taken to external parameters through the derivative of the
+// mapping at the solution and scaled by chi^2 / (ndata - nvary).
+//
+// Layout.  One warp runs one chain of fits (a fit_multik sweep warm-starts
+// each fit from the previous result, so a chain is sequential).  The n x n
+// state (the triangular factor, the step, the trust region) is computed by
+// all 32 lanes identically; the m data points are spread over the lanes
+// (point i on lane i % 32) and every sum over them is an xor-butterfly
+// reduction, which leaves the same bits in every lane.  The Jacobian columns
+// and the two residual vectors live in a per-warp slot of the workspace; each
+// element is only touched by the lane that owns its point, so the only
+// exchanges between lanes are the reductions and the shuffles of row j of the
+// factor.  The number of varying parameters is a template argument, so the
+// small arrays stay in registers.
+//
+// The files including this header are compiled without multiply-add
+// contraction (-fmad=false), as the host arithmetic they follow has none.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <algorithm>
+#include <stdint.h>
+#include "fddm_b200.h"
+#include "fddm_internal.h"
+
+namespace fddm {
+namespace fitlm {
+
+constexpr int kMaxP = 8;         // parameters of the largest model (7) rounded up
+constexpr int kWarpsPerCta = 4;
+constexpr double kEpsMch = 2.220446049250313e-16;       // DBL_EPSILON
+constexpr double kDwarf = 2.2250738585072014e-308;      // DBL_MIN
+
+enum Status : int { kOk = 0, kNonFinite = 1, kAborted = 2, kInvalid = 3 };
+
+__host__ __device__ inline int model_nparams(int model) {
+  switch (model) {
+    case FDDM_FIT_GENERIC_EXP_ISF: return 3;
+    case FDDM_FIT_DOUBLE_EXP_ISF: return 6;
+    case FDDM_FIT_FLORY_SCHULZ_ISF: return 3;
+    case FDDM_FIT_GENERIC_EXP_SF: return 4;
+    case FDDM_FIT_DOUBLE_EXP_SF: return 7;
+    case FDDM_FIT_FLORY_SCHULZ_SF: return 4;
+    case FDDM_FIT_SIMPLE_EXP: return 2;
+    case FDDM_FIT_SIMPLE_SF: return 3;
+    default: return 0;
+  }
+}
+
+// b ** e as numpy evaluates an array to a scalar power: exponents 1, 2, 0.5,
+// -1 and 0 take exact shortcuts (positive, square, sqrt, reciprocal, ones)
+__device__ __forceinline__ double npow(double b, double e) {
+  if (e == 1.0) return b;
+  if (e == 2.0) return b * b;
+  if (e == 0.5) return sqrt(b);
+  if (e == -1.0) return 1.0 / b;
+  if (e == 0.0) return 1.0;
+  return pow(b, e);
+}
+
+// The model functions of fit_models.py and fit.py, in their operation order.
+// p holds the parameters in the order of the Python function's arguments.
+__device__ __forceinline__ double model_eval(int model, double x, const double (&p)[kMaxP]) {
+  switch (model) {
+    case FDDM_FIT_GENERIC_EXP_ISF:  // A exp(-(x Gamma)^beta)                      fit_models.py:515-549
+      return p[0] * exp(-npow(x * p[1], p[2]));
+    case FDDM_FIT_DOUBLE_EXP_ISF: {  // A (alpha e1 + (1 - alpha) e2)               fit_models.py:615-659
+      const double e1 = exp(-npow(x * p[1], p[2])), e2 = exp(-npow(x * p[3], p[4]));
+      return p[0] * (p[5] * e1 + (1.0 - p[5]) * e2);
+    }
+    case FDDM_FIT_FLORY_SCHULZ_ISF: {  // A (1 + sigma^2 Gamma x)^(-1/sigma^2)      fit_models.py:690-735
+      const double s2 = p[2] * p[2];
+      return p[0] * npow(1.0 + s2 * p[1] * x, -1.0 / s2);
+    }
+    case FDDM_FIT_GENERIC_EXP_SF:  // A (1 - exp(-(x Gamma)^beta)) + B               fit_models.py:774-808
+      return p[0] * (1.0 - exp(-npow(x * p[2], p[3]))) + p[1];
+    case FDDM_FIT_DOUBLE_EXP_SF: {  // A (1 - (alpha e1 + (1 - alpha) e2)) + B      fit_models.py:890-936
+      const double e1 = exp(-npow(x * p[2], p[3])), e2 = exp(-npow(x * p[4], p[5]));
+      return p[0] * (1.0 - (p[6] * e1 + (1.0 - p[6]) * e2)) + p[1];
+    }
+    case FDDM_FIT_FLORY_SCHULZ_SF: {  // A (1 - (1 + sigma^2 Gamma x)^(-1/sigma^2)) + B  fit_models.py:971-1017
+      const double s2 = p[3] * p[3];
+      return p[0] * (1.0 - npow(1.0 + s2 * p[2] * x, -1.0 / s2)) + p[1];
+    }
+    case FDDM_FIT_SIMPLE_EXP:  // amplitude exp(-dt / tau)                           fit.py:67-74
+      return p[1] * exp(-x / p[0]);
+    default:  // FDDM_FIT_SIMPLE_SF: A (1 - exp(-dt / tau)) + B                       fit.py:84-88
+      return p[0] * (1.0 - exp(-x / p[2])) + p[1];
+  }
+}
+
+// lmfit's parameter mappings (kind: 0 unbounded, 1 lower bound, 2 upper bound, 3 both)
+__device__ __forceinline__ double from_internal(double u, double lo, double hi, int kind) {
+  switch (kind) {
+    case 0: return u;
+    case 1: return lo - 1.0 + sqrt(u * u + 1.0);
+    case 2: return hi + 1.0 - sqrt(u * u + 1.0);
+    default: return lo + (sin(u) + 1.0) * (hi - lo) / 2.0;
+  }
+}
+
+__device__ __forceinline__ double to_internal(double v, double lo, double hi, int kind) {
+  switch (kind) {
+    case 0: return v;
+    case 1: { const double t = v - lo + 1.0; return sqrt(t * t - 1.0); }
+    case 2: { const double t = hi - v + 1.0; return sqrt(t * t - 1.0); }
+    default: return asin(2.0 * (v - lo) / (hi - lo) - 1.0);
+  }
+}
+
+__device__ __forceinline__ double scale_gradient(double u, double lo, double hi, int kind) {
+  switch (kind) {
+    case 0: return 1.0;
+    case 1: return u / sqrt(u * u + 1.0);
+    case 2: return -u / sqrt(u * u + 1.0);
+    default: return cos(u) * (hi - lo) / 2.0;
+  }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// a[i] for a runtime index i over a register array (an unrolled select keeps a in registers)
+template <int N, class T>
+__device__ __forceinline__ T sel(const T (&a)[N], int i) {
+  T r = a[0];
+#pragma unroll
+  for (int k = 1; k < N; ++k)
+    if (k == i) r = a[k];
+  return r;
+}
+
+template <int N, class T>
+__device__ __forceinline__ void put(T (&a)[N], int i, T v) {
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+    if (k == i) a[k] = v;
+}
+
+template <int N>
+__device__ __forceinline__ double norm_n(const double (&v)[N]) {
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < N; ++k) s += v[k] * v[k];
+  return sqrt(s);
+}
+
+struct Batch {
+  int model, np, m;
+  const double* x;
+  const double* y;
+  uint64_t ldy;
+  int ny;  // rows of y
+  const double* w;
+  uint64_t ldw;
+  int nw;  // rows of w
+  int nprob;
+  const int32_t* problems;  // [nprob][4]: y row, w row (-1: none), pred (-1: none), vary mask
+  const int32_t* chain_off;
+  const int32_t* chain_list;
+  int nchains;
+  const double* init;
+  const double* lo;
+  const double* hi;
+  double ftol, xtol, gtol, epsfcn, factor;
+  long long max_nfev;
+  double* values;
+  double* stderr_;
+  double* chisqr;
+  int32_t* nfev;
+  int32_t* info;
+  int32_t* status;
+  double* residual;  // [nprob][m] or null
+  double* ws;
+  size_t slot_doubles;
+  int nslots;
+};
+
+// One fit.  NV: varying parameters.
+template <int NV>
+struct Fit {
+  const Batch& b;
+  const int lane;
+  const double* y;
+  const double* w;
+  double* fj[NV];
+  double pe[kMaxP];  // external values (fixed ones are constant)
+  int vix[NV];       // parameter index of each varying parameter
+  double lo[NV], hi[NV];
+  int kind[NV];
+  long long nfev = 0;
+  int status = kOk;
+
+  __device__ Fit(const Batch& b_, int lane_) : b(b_), lane(lane_) {}
+
+  __device__ void set_point(const double (&u)[NV]) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double v = from_internal(u[k], lo[k], hi[k], kind[k]);
+#pragma unroll
+      for (int p = 0; p < kMaxP; ++p)
+        if (p == vix[k]) pe[p] = v;
+    }
+  }
+
+  // residuals (model - y) * w at the current pe into out; returns the sum of squares.
+  // With fd != 0, out[i] = (r_i - fv[i]) / fd (a Jacobian column) and the sum is over those.
+  __device__ double evaluate(double* out, const double* fv, double fd) {
+    double s = 0.0;
+    bool bad = false;
+    for (int i = lane; i < b.m; i += 32) {
+      double r = model_eval(b.model, b.x[i], pe) - y[i];
+      if (w) r = r * w[i];
+      bad |= !isfinite(r);
+      if (fd != 0.0) r = (r - fv[i]) / fd;
+      out[i] = r;
+      s += r * r;
+    }
+    if (__any_sync(0xffffffffu, bad)) status = kNonFinite;
+    ++nfev;
+    if (nfev > b.max_nfev && status == kOk) status = kAborted;
+    return warp_sum(s);
+  }
+};
+
+// Householder QR with column pivoting of the NV columns fj (MINPACK qrfac with
+// pivoting), each reflection also applied to wt (a copy of the residuals) as
+// it is formed.  colsq: squared column norms.  Outputs: R (upper triangle, by
+// pivot position), ipvt (position -> parameter), acnorm (by parameter), qtf.
+template <int NV>
+__device__ void qr_pivot(Fit<NV>& F, const double (&colsq)[NV], double* wt, double (&R)[NV][NV], int (&ipvt)[NV],
+                         double (&acnorm)[NV], double (&qtf)[NV]) {
+  const int m = F.b.m, lane = F.lane;
+  double rdiag[NV], wa[NV];
+  bool recomp[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    ipvt[k] = k;
+    acnorm[k] = sqrt(colsq[k]);
+    rdiag[k] = acnorm[k];
+    wa[k] = acnorm[k];
+    recomp[k] = false;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) R[i][k] = 0.0;
+  }
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    // squared norms of the columns below row j-1, and row j (lane j owns point j)
+    double fresh[NV], rowj[NV];
+    if (j == 0) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) fresh[k] = colsq[k];
+    } else {
+      double part[NV];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) part[k] = 0.0;
+      for (int i = lane; i < m; i += 32) {
+        if (i < j) continue;
+#pragma unroll
+        for (int k = j; k < NV; ++k) {
+          const double v = F.fj[ipvt[k]][i];
+          part[k] += v * v;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < NV; ++k) fresh[k] = k >= j ? warp_sum(part[k]) : 0.0;
+    }
+#pragma unroll
+    for (int k = j; k < NV; ++k) rowj[k] = __shfl_sync(0xffffffffu, lane == j ? F.fj[ipvt[k]][j] : 0.0, j);
+    const double wj = __shfl_sync(0xffffffffu, lane == j ? wt[j] : 0.0, j);
+    // norms flagged at the previous step are taken afresh (MINPACK recomputes them there)
+#pragma unroll
+    for (int k = j; k < NV; ++k)
+      if (recomp[k]) {
+        rdiag[k] = sqrt(fresh[k]);
+        wa[k] = rdiag[k];
+        recomp[k] = false;
+      }
+    // pivot: the first largest remaining norm
+    int kmax = j;
+#pragma unroll
+    for (int k = j + 1; k < NV; ++k)
+      if (rdiag[k] > sel(rdiag, kmax)) kmax = k;
+    if (kmax != j) {
+#pragma unroll
+      for (int k = j + 1; k < NV; ++k)
+        if (k == kmax) {
+          int ti = ipvt[j]; ipvt[j] = ipvt[k]; ipvt[k] = ti;
+          double t = fresh[j]; fresh[j] = fresh[k]; fresh[k] = t;
+          t = rowj[j]; rowj[j] = rowj[k]; rowj[k] = t;
+          rdiag[k] = rdiag[j];
+          wa[k] = wa[j];
+#pragma unroll
+          for (int i = 0; i < j; ++i) { t = R[i][j]; R[i][j] = R[i][k]; R[i][k] = t; }
+        }
+    }
+    double ajnorm = sqrt(fresh[j]);
+    if (ajnorm != 0.0) {
+      if (rowj[j] < 0.0) ajnorm = -ajnorm;
+      const double vjj = rowj[j] / ajnorm + 1.0;
+      double* cj = F.fj[ipvt[j]];
+      double dot[NV], dw = 0.0;
+#pragma unroll
+      for (int k = 0; k < NV; ++k) dot[k] = 0.0;
+      for (int i = lane; i < m; i += 32) {
+        if (i < j) continue;
+        double v = cj[i] / ajnorm;
+        if (i == j) v = v + 1.0;
+        cj[i] = v;
+        dw += v * wt[i];
+#pragma unroll
+        for (int k = j + 1; k < NV; ++k) dot[k] += v * F.fj[ipvt[k]][i];
+      }
+      const double tw = -warp_sum(dw) / vjj;
+      double tk[NV];
+#pragma unroll
+      for (int k = j + 1; k < NV; ++k) tk[k] = warp_sum(dot[k]) / vjj;
+      for (int i = lane; i < m; i += 32) {
+        if (i < j) continue;
+        const double v = cj[i];
+        wt[i] = wt[i] + v * tw;
+#pragma unroll
+        for (int k = j + 1; k < NV; ++k) F.fj[ipvt[k]][i] = F.fj[ipvt[k]][i] - tk[k] * v;
+      }
+      qtf[j] = wj + vjj * tw;
+#pragma unroll
+      for (int k = j + 1; k < NV; ++k) {
+        R[j][k] = rowj[k] - tk[k] * vjj;
+        if (rdiag[k] != 0.0) {
+          const double t = R[j][k] / rdiag[k];
+          rdiag[k] *= sqrt(fmax(0.0, 1.0 - t * t));
+          const double q = rdiag[k] / wa[k];
+          if (0.05 * (q * q) <= kEpsMch) recomp[k] = true;
+        }
+      }
+    } else {
+      qtf[j] = wj;
+#pragma unroll
+      for (int k = j + 1; k < NV; ++k) R[j][k] = rowj[k];
+    }
+    rdiag[j] = -ajnorm;
+    R[j][j] = rdiag[j];
+  }
+}
+
+// MINPACK qrsolv: given R (by pivot position), ipvt, the diagonal d (by
+// parameter) and qtb, solve min |[R P^T; D] x - [qtb; 0]|.  S receives the
+// triangular factor of the augmented system (transposed, below the diagonal)
+// and sdiag its diagonal.
+template <int NV>
+__device__ void qrsolv(const double (&R)[NV][NV], const int (&ipvt)[NV], const double (&d)[NV], const double (&qtb)[NV],
+                       double (&x)[NV], double (&S)[NV][NV], double (&sdiag)[NV]) {
+  double wa[NV];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+#pragma unroll
+    for (int i = j; i < NV; ++i) S[i][j] = R[j][i];
+    wa[j] = qtb[j];
+  }
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    const double dl = sel(d, ipvt[j]);
+    if (dl != 0.0) {
+#pragma unroll
+      for (int k = j; k < NV; ++k) sdiag[k] = 0.0;
+      sdiag[j] = dl;
+      double qtbpj = 0.0;
+#pragma unroll
+      for (int k = j; k < NV; ++k) {
+        if (sdiag[k] == 0.0) continue;
+        double sn, cs;
+        if (fabs(S[k][k]) < fabs(sdiag[k])) {
+          const double cotan = S[k][k] / sdiag[k];
+          sn = 0.5 / sqrt(0.25 + 0.25 * (cotan * cotan));
+          cs = sn * cotan;
+        } else {
+          const double tn = sdiag[k] / S[k][k];
+          cs = 0.5 / sqrt(0.25 + 0.25 * (tn * tn));
+          sn = cs * tn;
+        }
+        S[k][k] = cs * S[k][k] + sn * sdiag[k];
+        const double t = cs * wa[k] + sn * qtbpj;
+        qtbpj = -sn * wa[k] + cs * qtbpj;
+        wa[k] = t;
+#pragma unroll
+        for (int i = k + 1; i < NV; ++i) {
+          const double u = cs * S[i][k] + sn * sdiag[i];
+          sdiag[i] = -sn * S[i][k] + cs * sdiag[i];
+          S[i][k] = u;
+        }
+      }
+    }
+    sdiag[j] = S[j][j];
+    S[j][j] = R[j][j];
+  }
+  int nsing = NV;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    if (sdiag[j] == 0.0 && nsing == NV) nsing = j;
+    if (nsing < NV) wa[j] = 0.0;
+  }
+#pragma unroll
+  for (int j = NV - 1; j >= 0; --j) {
+    if (j >= nsing) continue;
+    double s = 0.0;
+#pragma unroll
+    for (int i = j + 1; i < NV; ++i)
+      if (i < nsing) s += S[i][j] * wa[i];
+    wa[j] = (wa[j] - s) / sdiag[j];
+  }
+#pragma unroll
+  for (int j = 0; j < NV; ++j) put(x, ipvt[j], wa[j]);
+}
+
+// MINPACK lmpar: the Levenberg-Marquardt parameter for the trust radius delta
+// and the step x (by parameter); returns the new parameter.
+template <int NV>
+__device__ double lmpar(const double (&R)[NV][NV], const int (&ipvt)[NV], const double (&diag)[NV],
+                        const double (&qtb)[NV], double delta, double par, double (&x)[NV]) {
+  double wa1[NV], wa2[NV];
+  int nsing = NV;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    wa1[j] = qtb[j];
+    if (R[j][j] == 0.0 && nsing == NV) nsing = j;
+    if (nsing < NV) wa1[j] = 0.0;
+  }
+#pragma unroll
+  for (int j = NV - 1; j >= 0; --j) {
+    if (j >= nsing) continue;
+    wa1[j] = wa1[j] / R[j][j];
+    const double t = wa1[j];
+#pragma unroll
+    for (int i = 0; i < j; ++i) wa1[i] -= R[i][j] * t;
+  }
+#pragma unroll
+  for (int j = 0; j < NV; ++j) put(x, ipvt[j], wa1[j]);
+#pragma unroll
+  for (int j = 0; j < NV; ++j) wa2[j] = diag[j] * x[j];
+  double dxnorm = norm_n(wa2);
+  double fp = dxnorm - delta;
+  if (fp <= 0.1 * delta) return 0.0;
+  // lower bound from the Newton step (when the Jacobian has full rank)
+  double parl = 0.0;
+  if (nsing >= NV) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      const int l = ipvt[j];
+      wa1[j] = sel(diag, l) * (sel(wa2, l) / dxnorm);
+    }
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      double s = 0.0;
+#pragma unroll
+      for (int i = 0; i < j; ++i) s += R[i][j] * wa1[i];
+      wa1[j] = (wa1[j] - s) / R[j][j];
+    }
+    const double t = norm_n(wa1);
+    parl = ((fp / delta) / t) / t;
+  }
+  // upper bound
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i <= j; ++i) s += R[i][j] * qtb[i];
+    wa1[j] = s / sel(diag, ipvt[j]);
+  }
+  const double gnorm = norm_n(wa1);
+  double paru = gnorm / delta;
+  if (paru == 0.0) paru = kDwarf / fmin(delta, 0.1);
+  par = fmax(par, parl);
+  par = fmin(par, paru);
+  if (par == 0.0) par = gnorm / dxnorm;
+  double S[NV][NV], sdiag[NV];
+  for (int iter = 1;; ++iter) {
+    if (par == 0.0) par = fmax(kDwarf, 0.001 * paru);
+    const double sp = sqrt(par);
+#pragma unroll
+    for (int j = 0; j < NV; ++j) wa1[j] = sp * diag[j];
+    qrsolv(R, ipvt, wa1, qtb, x, S, sdiag);
+#pragma unroll
+    for (int j = 0; j < NV; ++j) wa2[j] = diag[j] * x[j];
+    dxnorm = norm_n(wa2);
+    const double fp_old = fp;
+    fp = dxnorm - delta;
+    if (fabs(fp) <= 0.1 * delta || (parl == 0.0 && fp <= fp_old && fp_old < 0.0) || iter == 10) break;
+    // Newton correction
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      const int l = ipvt[j];
+      wa1[j] = sel(diag, l) * (sel(wa2, l) / dxnorm);
+    }
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      wa1[j] = wa1[j] / sdiag[j];
+      const double t = wa1[j];
+#pragma unroll
+      for (int i = j + 1; i < NV; ++i) wa1[i] -= S[i][j] * t;
+    }
+    const double t = norm_n(wa1);
+    const double parc = ((fp / delta) / t) / t;
+    if (fp > 0.0) parl = fmax(parl, par);
+    if (fp < 0.0) paru = fmin(paru, par);
+    par = fmax(parl, par + parc);
+  }
+  return par;
+}
+
+// lmdif on one problem; u holds the internal starting point and receives the result.
+template <int NV>
+__device__ void lmdif(Fit<NV>& F, double (&u)[NV], double*& fv, double*& wt, double& fsq, int& info,
+                      double (&R)[NV][NV], int (&ipvt)[NV]) {
+  const Batch& b = F.b;
+  const double eps = sqrt(fmax(b.epsfcn, kEpsMch));
+  F.set_point(u);
+  fsq = F.evaluate(fv, nullptr, 0.0);
+  info = 0;
+  if (F.status != kOk) return;
+  double fnorm = sqrt(fsq);
+  double par = 0.0, delta = 0.0, xnorm = 0.0;
+  double diag[NV], acnorm[NV], qtf[NV];
+  for (int iter = 1;;) {
+    // forward-difference Jacobian
+    double colsq[NV];
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      const double t = u[j];
+      double h = eps * fabs(t);
+      if (h == 0.0) h = eps;
+      u[j] = t + h;
+      F.set_point(u);
+      colsq[j] = F.evaluate(F.fj[j], fv, h);
+      u[j] = t;
+      if (F.status != kOk) return;
+    }
+    for (int i = F.lane; i < b.m; i += 32) wt[i] = fv[i];
+    qr_pivot(F, colsq, wt, R, ipvt, acnorm, qtf);
+    if (iter == 1) {
+#pragma unroll
+      for (int j = 0; j < NV; ++j) diag[j] = acnorm[j] == 0.0 ? 1.0 : acnorm[j];
+      double t[NV];
+#pragma unroll
+      for (int j = 0; j < NV; ++j) t[j] = diag[j] * u[j];
+      xnorm = norm_n(t);
+      delta = b.factor * xnorm;
+      if (delta == 0.0) delta = b.factor;
+    }
+    // scaled gradient
+    double gnorm = 0.0;
+    if (fnorm != 0.0) {
+#pragma unroll
+      for (int j = 0; j < NV; ++j) {
+        const double an = sel(acnorm, ipvt[j]);
+        if (an != 0.0) {
+          double s = 0.0;
+#pragma unroll
+          for (int i = 0; i <= j; ++i) s += R[i][j] * (qtf[i] / fnorm);
+          gnorm = fmax(gnorm, fabs(s / an));
+        }
+      }
+    }
+    if (gnorm <= b.gtol) info = 4;
+    if (info != 0) return;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) diag[j] = fmax(diag[j], acnorm[j]);
+    for (;;) {
+      double p[NV], ut[NV], dp[NV];
+      par = lmpar(R, ipvt, diag, qtf, delta, par, p);
+#pragma unroll
+      for (int j = 0; j < NV; ++j) {
+        p[j] = -p[j];
+        ut[j] = u[j] + p[j];
+        dp[j] = diag[j] * p[j];
+      }
+      const double pnorm = norm_n(dp);
+      if (iter == 1) delta = fmin(delta, pnorm);
+      F.set_point(ut);
+      const double fsq1 = F.evaluate(wt, nullptr, 0.0);
+      if (F.status != kOk) return;  // the result stays at the last accepted point
+      const double fnorm1 = sqrt(fsq1);
+      double actred = -1.0;
+      if (0.1 * fnorm1 < fnorm) {
+        const double q = fnorm1 / fnorm;
+        actred = 1.0 - q * q;
+      }
+      double wa3[NV];
+#pragma unroll
+      for (int j = 0; j < NV; ++j) wa3[j] = 0.0;
+#pragma unroll
+      for (int j = 0; j < NV; ++j) {
+        const double t = sel(p, ipvt[j]);
+#pragma unroll
+        for (int i = 0; i <= j; ++i) wa3[i] += R[i][j] * t;
+      }
+      const double temp1 = norm_n(wa3) / fnorm;
+      const double temp2 = (sqrt(par) * pnorm) / fnorm;
+      const double prered = temp1 * temp1 + temp2 * temp2 / 0.5;
+      const double dirder = -(temp1 * temp1 + temp2 * temp2);
+      const double ratio = prered != 0.0 ? actred / prered : 0.0;
+      if (ratio <= 0.25) {
+        double t = actred >= 0.0 ? 0.5 : 0.5 * dirder / (dirder + 0.5 * actred);
+        if (0.1 * fnorm1 >= fnorm || t < 0.1) t = 0.1;
+        delta = t * fmin(delta, pnorm / 0.1);
+        par = par / t;
+      } else if (par == 0.0 || ratio >= 0.75) {
+        delta = pnorm / 0.5;
+        par = 0.5 * par;
+      }
+      if (ratio >= 1e-4) {
+        double t[NV];
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+          u[j] = ut[j];
+          t[j] = diag[j] * u[j];
+        }
+        double* s = fv; fv = wt; wt = s;
+        xnorm = norm_n(t);
+        fnorm = fnorm1;
+        fsq = fsq1;
+        ++iter;
+      }
+      const bool fconv = fabs(actred) <= b.ftol && prered <= b.ftol && 0.5 * ratio <= 1.0;
+      if (fconv) info = 1;
+      if (delta <= b.xtol * xnorm) info = fconv ? 3 : 2;
+      if (info != 0) return;
+      if (fabs(actred) <= kEpsMch && prered <= kEpsMch && 0.5 * ratio <= 1.0) info = 6;
+      if (delta <= kEpsMch * xnorm) info = 7;
+      if (gnorm <= kEpsMch) info = 8;
+      if (info != 0) return;
+      if (ratio >= 1e-4) break;
+    }
+  }
+}
+
+template <int NV>
+__device__ void run_problem(const Batch& b, int prob, double* slot, int lane) {
+  const int32_t* pr = b.problems + 4 * (size_t)prob;
+  const int yrow = pr[0], wrow = pr[1], pred = pr[2];
+  const uint32_t vary = (uint32_t)pr[3];
+  // a problem naming a row or a predecessor that does not exist, or varying another number of
+  // parameters than the launch, is not fitted
+  if (yrow < 0 || yrow >= b.ny || wrow >= b.nw || (wrow >= 0 && !b.w) || pred >= b.nprob ||
+      __popc(vary & ((1u << b.np) - 1u)) != NV || (vary >> b.np) != 0u) {
+    if (lane == 0) {
+      for (int p = 0; p < b.np; ++p) {
+        b.values[(size_t)prob * b.np + p] = NAN;
+        b.stderr_[(size_t)prob * b.np + p] = NAN;
+      }
+      b.chisqr[prob] = NAN;
+      b.nfev[prob] = 0;
+      b.info[prob] = 0;
+      b.status[prob] = kInvalid;
+    }
+    __syncwarp();
+    return;
+  }
+  Fit<NV> F(b, lane);
+  F.y = b.y + (size_t)yrow * b.ldy;
+  F.w = wrow >= 0 ? b.w + (size_t)wrow * b.ldw : nullptr;
+  double* fv = slot;
+  double* wt = slot + b.m;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) F.fj[k] = slot + (size_t)(2 + k) * b.m;
+  // starting values: the predecessor's result for the varying parameters, clipped into the bounds
+  const double* ini = b.init + (size_t)prob * b.np;
+  const double* plo = b.lo + (size_t)prob * b.np;
+  const double* phi = b.hi + (size_t)prob * b.np;
+  double u[NV];
+  int nv = 0;
+#pragma unroll
+  for (int p = 0; p < kMaxP; ++p) {
+    if (p >= b.np) { F.pe[p] = 0.0; continue; }
+    const bool vp = (vary >> p) & 1u;
+    double v = (vp && pred >= 0) ? b.values[(size_t)pred * b.np + p] : ini[p];
+    const double l = plo[p], h = phi[p];
+    if (v > h) v = h;
+    if (v < l) v = l;
+    F.pe[p] = v;
+    if (vp) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+        if (k == nv) {
+          F.vix[k] = p;
+          F.lo[k] = l;
+          F.hi[k] = h;
+          F.kind[k] = (l == -INFINITY ? 0 : 1) + (h == INFINITY ? 0 : 2);
+          u[k] = to_internal(v, l, h, F.kind[k]);
+        }
+      ++nv;
+    }
+  }
+  double fsq = 0.0, R[NV][NV];
+  int info = 0, ipvt[NV];
+  lmdif(F, u, fv, wt, fsq, info, R, ipvt);
+  F.set_point(u);
+  // standard errors: inv(R'^T R') with R' = R / scale_gradient (by column), times chi^2 / nfree.
+  // As with numpy's inv there: entries that are not finite give NaN errors (fixed parameters 0); an
+  // exactly singular R'^T R gives no covariance at all (every error -1, reported as None).
+  double se[NV];
+  int cov = F.status == kOk ? 0 : 2;  // 0 exists, 1 not finite, 2 none
+  if (cov == 0) {
+    double Rp[NV][NV], Ui[NV][NV];
+    bool singular = false;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      const int l = ipvt[j];
+      double g = 0.0;
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+        if (k == l) g = scale_gradient(u[k], F.lo[k], F.hi[k], F.kind[k]);
+#pragma unroll
+      for (int i = 0; i < NV; ++i) {
+        Rp[i][j] = i <= j ? R[i][j] / g : 0.0;
+        if (!isfinite(Rp[i][j])) cov = 1;
+      }
+      if (Rp[j][j] == 0.0) singular = true;
+    }
+    if (cov == 0 && singular) cov = 2;
+    if (cov == 0) {
+      // Ui = Rp^{-1} (upper triangular, back substitution column by column)
+#pragma unroll
+      for (int c = 0; c < NV; ++c) {
+#pragma unroll
+        for (int i = NV - 1; i >= 0; --i) {
+          double s = i == c ? 1.0 : 0.0;
+#pragma unroll
+          for (int k = i + 1; k < NV; ++k) s -= Rp[i][k] * Ui[k][c];
+          Ui[i][c] = i <= c ? s / Rp[i][i] : 0.0;
+        }
+      }
+      const int nfree = b.m - NV;
+      const double redchi = fsq / (double)(nfree > 1 ? nfree : 1);
+      // variance of the parameter at position i: row i of Ui squared
+#pragma unroll
+      for (int i = 0; i < NV; ++i) {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) s += Ui[i][k] * Ui[i][k];
+        put(se, ipvt[i], sqrt(s * redchi));
+      }
+    } else if (cov == 1) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) se[k] = NAN;
+    }
+  }
+  if (lane == 0) {
+    double* vo = b.values + (size_t)prob * b.np;
+    double* so = b.stderr_ + (size_t)prob * b.np;
+#pragma unroll
+    for (int p = 0; p < kMaxP; ++p) {
+      if (p >= b.np) break;
+      vo[p] = F.pe[p];
+      double s = cov == 2 ? -1.0 : 0.0;  // fixed parameters: 0 when a covariance exists
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+        if (F.vix[k] == p && cov != 2) s = se[k];
+      so[p] = s;
+    }
+    b.chisqr[prob] = fsq;
+    b.nfev[prob] = (int32_t)F.nfev;
+    b.info[prob] = F.status == kAborted ? -1 : info;
+    b.status[prob] = F.status;
+  }
+  if (b.residual)
+    for (int i = lane; i < b.m; i += 32) b.residual[(size_t)prob * b.m + i] = fv[i];
+  __syncwarp();
+}
+
+template <int NV>
+__global__ void __launch_bounds__(32 * kWarpsPerCta) k_fit_lm(Batch b) {
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+  if (gw >= b.nslots) return;
+  double* slot = b.ws + (size_t)gw * b.slot_doubles;
+  for (int c = gw; c < b.nchains; c += b.nslots) {
+    bool stop = false;
+    for (int e = b.chain_off[c]; e < b.chain_off[c + 1] && !stop; ++e) {
+      const int prob = b.chain_list[e];
+      if (prob < 0 || prob >= b.nprob) break;  // not a problem: the chain ends
+      run_problem<NV>(b, prob, slot, lane);
+      // a fit that raised in the reference ends its sweep there
+      stop = b.status[prob] == kNonFinite || b.status[prob] == kInvalid;
+    }
+  }
+}
+
+template <int NV>
+cudaError_t launch(const Batch& b, unsigned grid, cudaStream_t st) {
+  k_fit_lm<NV><<<grid, 32 * kWarpsPerCta, 0, st>>>(b);
+  return cudaGetLastError();
+}
+
+// one launcher per number of varying parameters, each in its own translation unit
+cudaError_t launch_nv1(const Batch& b, unsigned grid, cudaStream_t st);
+cudaError_t launch_nv2(const Batch& b, unsigned grid, cudaStream_t st);
+cudaError_t launch_nv3(const Batch& b, unsigned grid, cudaStream_t st);
+cudaError_t launch_nv4(const Batch& b, unsigned grid, cudaStream_t st);
+cudaError_t launch_nv5(const Batch& b, unsigned grid, cudaStream_t st);
+cudaError_t launch_nv6(const Batch& b, unsigned grid, cudaStream_t st);
+cudaError_t launch_nv7(const Batch& b, unsigned grid, cudaStream_t st);
+
+}  // namespace fitlm
+}  // namespace fddm

@@ -1,0 +1,8 @@
+// Batched Levenberg-Marquardt fits with 3 varying parameters (kernel in fit_lm.cuh).
+#include "fit_lm.cuh"
+
+namespace fddm {
+namespace fitlm {
+cudaError_t launch_nv3(const Batch& b, unsigned grid, cudaStream_t st) { return launch<3>(b, grid, st); }
+}  // namespace fitlm
+}  // namespace fddm

@@ -1,0 +1,8 @@
+// Batched Levenberg-Marquardt fits with 6 varying parameters (kernel in fit_lm.cuh).
+#include "fit_lm.cuh"
+
+namespace fddm {
+namespace fitlm {
+cudaError_t launch_nv6(const Batch& b, unsigned grid, cudaStream_t st) { return launch<6>(b, grid, st); }
+}  // namespace fitlm
+}  // namespace fddm

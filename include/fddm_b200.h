@@ -327,6 +327,68 @@ int fddm_b200_last_input_path(void);
    sums taken from shared memory and no MMA: a lower bound on its time. */
 int fddm_b200_experiment_dft_stage(int variant, const void* d_rows, uint64_t npairs, void* d_out, void* stream);
 
+/* Batched Levenberg-Marquardt fits of the relaxation models: replaces the
+   lmfit Model.fit calls of the reference's fit_multik (src/python/fit.py:337,
+   :380) and fit (fit.py:188).  Each fit follows lmfit's default 'leastsq'
+   method: MINPACK's lmdif on lmfit's internal parameters (bounds mapped by
+   the MINUIT transformations), forward-difference Jacobian, lmfit's
+   tolerances, standard errors from inv(R^T R) scaled by chi^2 / nfree.
+   Models (parameters in the order of the reference functions' arguments):
+     FDDM_FIT_GENERIC_EXP_ISF   A, Gamma, beta        fit_models.py:515
+     FDDM_FIT_DOUBLE_EXP_ISF    A, Gamma1, beta1, Gamma2, beta2, alpha   :615
+     FDDM_FIT_FLORY_SCHULZ_ISF  A, Gamma, sigma       :690
+     FDDM_FIT_GENERIC_EXP_SF    A, B, Gamma, beta     :774
+     FDDM_FIT_DOUBLE_EXP_SF     A, B, Gamma1, beta1, Gamma2, beta2, alpha   :890
+     FDDM_FIT_FLORY_SCHULZ_SF   A, B, Gamma, sigma    :971
+     FDDM_FIT_SIMPLE_EXP        tau, amplitude        fit.py:67
+     FDDM_FIT_SIMPLE_SF         A, B, tau             fit.py:84
+   A problem is one curve: y row d_y + row*ldy of ny rows (m points at
+   abscissae d_x), weights row d_w + wrow*ldw of nw rows or none (residual
+   (model - y) * w), starting
+   values, bounds (+-INFINITY for none) and the mask of varying parameters.
+   d_problems holds 4 int32 per problem: y row, weight row (-1: none), pred
+   (-1: none), vary mask (bit p: parameter p varies; the same number nvary of
+   set bits in every problem).  With pred >= 0 the varying parameters start
+   from problem pred's fitted values instead of d_init (fit_multik's warm
+   start); pred must come earlier in the same chain or have been fitted by an
+   earlier call.  Starting values are clipped into [min, max] as lmfit does.
+   Chains: chain c runs problems d_chain_problems[d_chain_offsets[c] ..
+   d_chain_offsets[c+1]-1] in order on one warp; chains run concurrently.
+   d_init, d_min, d_max, d_values, d_stderr: [nproblems][nparams] doubles.
+   options (host, 6 doubles): ftol, xtol, gtol, epsfcn, factor, max_nfev
+   (<= 0: 2000*(nvary+1)); lmfit's defaults are 1e-7, 1e-7, 1e-7, 0, 100, 0.
+   Outputs per problem: fitted values (fixed parameters keep theirs),
+   standard errors (0 for fixed parameters; NaN where the covariance has
+   entries that are not finite, e.g. a parameter exactly on a bound; -1 for
+   every parameter when R^T R is exactly singular or the fit did not
+   finish), chi^2, function evaluations, MINPACK's info (1-4
+   converged, 6-8 tolerance too small, -1 aborted), status (0 done, 1 a
+   residual was not finite: the reference raises ValueError there and the
+   chain stops, 2 aborted after max_nfev evaluations, 3 not fitted: a row or
+   predecessor out of range or another number of varying parameters; a
+   chain also ends at an entry that is not a problem), and optionally the
+   final residuals ([nproblems][m], d_residual may be NULL).
+   The workspace holds (2 + nparams) * m doubles per concurrently running
+   chain; fddm_b200_fit_workspace_bytes gives the size that runs every chain
+   at once (a smaller one runs fewer at a time, down to one). */
+#define FDDM_FIT_GENERIC_EXP_ISF 0
+#define FDDM_FIT_DOUBLE_EXP_ISF 1
+#define FDDM_FIT_FLORY_SCHULZ_ISF 2
+#define FDDM_FIT_GENERIC_EXP_SF 3
+#define FDDM_FIT_DOUBLE_EXP_SF 4
+#define FDDM_FIT_FLORY_SCHULZ_SF 5
+#define FDDM_FIT_SIMPLE_EXP 6
+#define FDDM_FIT_SIMPLE_SF 7
+int fddm_b200_fit_model_nparams(int model);
+int fddm_b200_fit_workspace_bytes(int model, uint64_t m, uint64_t nchains, uint64_t* bytes);
+int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, const double* d_y, uint64_t ldy, uint64_t ny,
+                     const double* d_w, uint64_t ldw, uint64_t nw, const int32_t* d_problems, uint64_t nproblems,
+                     const int32_t* d_chain_offsets,
+                     const int32_t* d_chain_problems, uint64_t nchains, int nvary, const double* d_init,
+                     const double* d_min, const double* d_max, const double* options, double* d_values,
+                     double* d_stderr, double* d_chisqr, int32_t* d_nfev, int32_t* d_info, int32_t* d_status,
+                     double* d_residual, void* d_workspace, uint64_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
