@@ -251,6 +251,96 @@ def azavg_record(out, nx: int, ny: int, device, bins: int = 512, reps: int = 3) 
         ok = ~torch.isnan(b)
         diff = max(diff, float(((a[ok] - b[ok]).abs() / b[ok].abs().clamp_min(1e-300)).max()))
     rec["fast_vs_exact_max_rel"] = diff
+    avg, err = res["exact"]
+    return rec, aa.AzimuthalAverage(avg.cpu().numpy(), err.cpu().numpy(), setup.k, None, setup.bin_edges)
+
+
+def fit_record(azavg, tau: np.ndarray, reps: int = 3) -> dict:
+    """fit_multik of the azimuthal average, as the reference's fit.py docstring sets it up.
+
+    Simple exponential structure function, weights 1 / err, B from the
+    "polyfit" noise estimate, A = 2 var - B and Gamma from the half-decay lag
+    at the reference k.  Bins whose error is 0 or not finite (the k = 0 bin
+    holds one pixel) are left out, as NaN rows.  Times the reference's
+    sequential sweep (``warm_start="chain"``) and every k from the fit at ref
+    (``"ref"``) on the device, best of ``reps``, and the oracle's sweep
+    (lmfit's wrapper restated around scipy's MINPACK, one host core).  Parity:
+    on the k the oracle determines well, the largest |device - oracle| over
+    max(1e-5 of the scale, 0.1 standard error) (1 = at the tolerance); on every
+    k, how many chi^2 agree within max(1e-9 relative, 0.05 reduced chi^2) and
+    how many are lower or higher on the device.
+    """
+    import copy as _copy
+
+    from fastddm_gb300 import fit as gfit
+    from fastddm_gb300 import fit_models, noise_est
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import fit_oracle as fo
+
+    a = _copy.copy(azavg)
+    a.tau = np.asarray(tau, dtype=np.float64)
+    data = a._data.copy()
+    bad = ~np.all(np.isfinite(a.err) & (a.err > 0), axis=1)
+    data[bad, 0] = np.nan
+    a._data = data
+    B_est, _ = noise_est.estimate_camera_noise(a, mode="polyfit")
+    valid = np.flatnonzero(~np.isnan(a.data[:, 0]))
+    ref = int(valid[len(valid) // 8])
+    A0 = 2.0 * a.var[ref] - B_est[ref]
+    half = np.abs((a.data[ref] - B_est[ref]) / A0 - 0.5)
+    G0 = 1.0 / a.tau[int(np.argmin(half))]
+    model = fit_models.simple_exponential_model
+    kw = dict(A=A0, B=B_est[ref], Gamma=G0, use_err=True)
+    rec = {"model": "simple_exponential_model", "k": int(valid.size), "lags": int(a.tau.size), "ref": ref,
+           "use_err": True}
+    tables = {}
+    for order in ("chain", "ref"):
+        best_dev, best_tot = float("inf"), float("inf")
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            tab, _ = gfit.fit_multik(a, model, ref, warm_start=order, **kw)
+            best_tot = min(best_tot, 1000 * (time.perf_counter() - t0))
+            best_dev = min(best_dev, tab.device_ms)
+        rec[f"{order}_device_ms"] = best_dev
+        rec[f"{order}_total_ms"] = best_tot
+        rec[f"{order}_success"] = int(np.sum(tab["success"]))
+        tables[order] = tab
+    func, names, _ = fo.MODELS["simple_exponential_model"]
+    params = fo.make_params("simple_exponential_model")
+    for n in ("A", "B", "Gamma"):
+        params[n]["value"] = float(kw[n])
+    t0 = time.perf_counter()
+    want = fo.fit_multik(func, names, params, a.tau, a.data, ref, err=a.err, use_err=True)
+    rec["oracle_chain_ms"] = 1000 * (time.perf_counter() - t0)
+    rec["oracle_cores"] = 1
+    got = tables["chain"]
+    ok = ~np.isnan(want["A"])
+    # parameters: on the k the oracle determines well (converged, every varying parameter to 10%)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        rel = np.maximum(want["A_stderr"] / np.abs(want["A"]), want["Gamma_stderr"] / np.abs(want["Gamma"]))
+    wd = ok & want["success"] & np.isfinite(rel) & (rel < 0.1)
+    worst = 0.0
+    for n in ("A", "B", "Gamma"):
+        scale = np.abs(want["A"][wd]) if n == "B" else np.abs(want[n][wd])
+        tol = np.maximum(1e-5 * scale, 0.1 * want[f"{n}_stderr"][wd])
+        if wd.any():
+            worst = max(worst, float(np.max(np.abs(got[n][wd] - want[n][wd]) / tol)))
+    rec["k_well_determined"] = int(wd.sum())
+    rec["parity_max_over_tol"] = worst
+    # chi^2 on every fitted k; elsewhere (only A + B determined: the decay is faster than the first lag
+    # or slower than the last) each run stops at its own point of a flat valley
+    w = 1.0 / a.err
+    chi_d = np.sum(((func(a.tau[None, :], got["A"][:, None], got["B"][:, None], got["Gamma"][:, None], 1.0)
+                     - a.data) * w) ** 2, axis=1)
+    chi_o = np.sum(((func(a.tau[None, :], want["A"][:, None], want["B"][:, None], want["Gamma"][:, None], 1.0)
+                     - a.data) * w) ** 2, axis=1)
+    ctol = np.maximum(1e-9 * chi_o, 0.05 * chi_o / (a.tau.size - 3))
+    rec["chi2_equal"] = int(np.sum(ok & (np.abs(chi_d - chi_o) <= ctol)))
+    rec["chi2_device_lower"] = int(np.sum(ok & (chi_o - chi_d > ctol)))
+    rec["chi2_device_higher"] = int(np.sum(ok & (chi_d - chi_o > ctol)))
+    rec["success_agree"] = bool(np.array_equal(got["success"], want["success"]))
+    rec["chain_vs_oracle"] = rec["oracle_chain_ms"] / rec["chain_device_ms"]
     return rec
 
 
@@ -527,9 +617,13 @@ def run_ours(args):
                      "sm_mhz": mhz, "source": ic["source"]}
 
     # the azimuthal average of the timed result (512 bins), both kernel orders
-    azavg = None
+    azavg = fits = None
     if rank == 0 and not args.no_check:
-        azavg = azavg_record(out, nx, ny, device)
+        azavg, aa_obj = azavg_record(out, nx, ny, device)
+        try:
+            fits = fit_record(aa_obj, np.asarray(lags, dtype=np.float64))
+        except (ValueError, RuntimeError) as e:  # recorded, not fatal to the structure-function line
+            fits = {"error": f"{type(e).__name__}: {e}"}
 
     # end to end through the public API: pinned host frames in, host result out
     e2e = None
@@ -622,7 +716,7 @@ def run_ours(args):
             "roofline": roofline, "issue_roofline": issue, "cpu_baseline": cpu, "e2e": e2e,
             "e2e_pageable": e2e_pageable, "accuracy": accuracy,
             "max_rel_err": accuracy["max_rel_err"] if accuracy else None, "f64_path": f64, "serve": serve,
-            "azimuthal_average": azavg,
+            "azimuthal_average": azavg, "fit_multik": fits,
             "clocks": clocks, "gpu_launches": launches,
         }
         print(json.dumps(line))

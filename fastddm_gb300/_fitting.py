@@ -98,13 +98,13 @@ class Parameters(dict):
         super().__setitem__(key, par)
 
     def update(self, other=(), **kw):
-        if isinstance(other, Parameter):
+        """Add or replace parameters; lmfit Parameter objects (anything with value, vary,
+        min, max and expr) are converted."""
+        if isinstance(other, Parameter) or hasattr(other, "vary") and hasattr(other, "name"):
             other = {other.name: other}
         items = other.items() if hasattr(other, "items") else other
-        for k, p in items:
-            self[k] = copy.copy(p)
-        for k, p in kw.items():
-            self[k] = copy.copy(p)
+        for k, p in list(items) + list(kw.items()):
+            self[k] = as_parameter(k, p)
         return self
 
     def valuesdict(self) -> Dict[str, float]:
@@ -124,6 +124,16 @@ class Parameters(dict):
         for k, p in self.items():
             se = "None" if p.stderr is None else f"{p.stderr:.5g}"
             print(f"{k:<10}{p.value!s:>14.12}{p.min!s:>12.8}{p.max!s:>12.8}{se:>12}{p.vary!s:>6}")
+
+
+def as_parameter(name: str, p) -> Parameter:
+    """A copy of ``p`` as a Parameter (``p`` may be an lmfit Parameter)."""
+    if isinstance(p, Parameter):
+        return copy.copy(p)
+    q = Parameter(name, value=getattr(p, "value", None), vary=getattr(p, "vary", True),
+                  min=getattr(p, "min", -INF), max=getattr(p, "max", INF), expr=getattr(p, "expr", None))
+    q.stderr = getattr(p, "stderr", None)
+    return q
 
 
 def _start_value(p: Parameter) -> float:

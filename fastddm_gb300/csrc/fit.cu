@@ -13,12 +13,19 @@ namespace {
 
 size_t slot_doubles(uint64_t m, int np) { return (size_t)(2 + np) * m; }
 
-int max_slots() {
+int sm_count() {
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  return (nsm > 0 ? nsm : 152) * 8 * fddm::fitlm::kWarpsPerCta;
+  return nsm > 0 ? nsm : 152;
 }
+
+// Warps per chain: with at most one chain per SM a chain takes a whole CTA (its per-point work
+// spread over the SM's four sub-partitions); with more, each warp runs its own chains.
+int group_warps(uint64_t nchains) { return nchains <= (uint64_t)sm_count() ? fddm::fitlm::kWarpsPerCta : 1; }
+
+// groups resident at once (8 CTAs per SM)
+uint64_t max_slots(int group) { return (uint64_t)sm_count() * 8 * (fddm::fitlm::kWarpsPerCta / group); }
 
 }  // namespace
 
@@ -31,7 +38,7 @@ extern "C" int fddm_b200_fit_workspace_bytes(int model, uint64_t m, uint64_t nch
   if (!bytes) return fail_with(FDDM_ERR_INVALID, "null pointer argument");
   const int np = fitlm::model_nparams(model);
   if (np == 0) return fail_with(FDDM_ERR_INVALID, "unknown fit model");
-  const uint64_t slots = std::min<uint64_t>(nchains, (uint64_t)max_slots());
+  const uint64_t slots = std::min<uint64_t>(nchains, max_slots(group_warps(nchains)));
   *bytes = (uint64_t)slot_doubles(m, np) * sizeof(double) * slots;
   return FDDM_OK;
 }
@@ -59,7 +66,8 @@ extern "C" int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, const 
     return fail_with(FDDM_ERR_INVALID, "null pointer argument");
   if (ldy < m || (d_w && ldw < m)) return fail_with(FDDM_ERR_INVALID, "row stride shorter than the data");
   const uint64_t per_slot = (uint64_t)slot_doubles(m, np) * sizeof(double);
-  const uint64_t slots = std::min<uint64_t>({nchains, (uint64_t)max_slots(), workspace_bytes / per_slot});
+  const int group = group_warps(nchains);
+  const uint64_t slots = std::min<uint64_t>({nchains, max_slots(group), workspace_bytes / per_slot});
   if (slots == 0) return fail_with(FDDM_ERR_NOMEM, "fit workspace smaller than one slot");
   fitlm::Batch b{};
   b.model = model;
@@ -96,17 +104,17 @@ extern "C" int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, const 
   b.ws = static_cast<double*>(d_workspace);
   b.slot_doubles = slot_doubles(m, np);
   b.nslots = (int)slots;
-  const unsigned grid = (unsigned)((slots + fitlm::kWarpsPerCta - 1) / fitlm::kWarpsPerCta);
+  const unsigned grid = (unsigned)(group > 1 ? slots : (slots + fitlm::kWarpsPerCta - 1) / fitlm::kWarpsPerCta);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t ce;
   switch (nvary) {
-    case 1: ce = fitlm::launch_nv1(b, grid, st); break;
-    case 2: ce = fitlm::launch_nv2(b, grid, st); break;
-    case 3: ce = fitlm::launch_nv3(b, grid, st); break;
-    case 4: ce = fitlm::launch_nv4(b, grid, st); break;
-    case 5: ce = fitlm::launch_nv5(b, grid, st); break;
-    case 6: ce = fitlm::launch_nv6(b, grid, st); break;
-    default: ce = fitlm::launch_nv7(b, grid, st); break;
+    case 1: ce = fitlm::launch_nv1(b, grid, group, st); break;
+    case 2: ce = fitlm::launch_nv2(b, grid, group, st); break;
+    case 3: ce = fitlm::launch_nv3(b, grid, group, st); break;
+    case 4: ce = fitlm::launch_nv4(b, grid, group, st); break;
+    case 5: ce = fitlm::launch_nv5(b, grid, group, st); break;
+    case 6: ce = fitlm::launch_nv6(b, grid, group, st); break;
+    default: ce = fitlm::launch_nv7(b, grid, group, st); break;
   }
   if (ce != cudaSuccess) return fail_with(FDDM_ERR_CUDA, cudaGetErrorString(ce));
   count_launches(1);

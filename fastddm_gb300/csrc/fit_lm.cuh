@@ -17,17 +17,29 @@
 // factorisation, taken to external parameters through the derivative of the
 // mapping at the solution and scaled by chi^2 / (ndata - nvary).
 //
-// Layout.  One warp runs one chain of fits (a fit_multik sweep warm-starts
-// each fit from the previous result, so a chain is sequential).  The n x n
-// state (the triangular factor, the step, the trust region) is computed by
-// all 32 lanes identically; the m data points are spread over the lanes
-// (point i on lane i % 32) and every sum over them is an xor-butterfly
-// reduction, which leaves the same bits in every lane.  The Jacobian columns
-// and the two residual vectors live in a per-warp slot of the workspace; each
-// element is only touched by the lane that owns its point, so the only
-// exchanges between lanes are the reductions and the shuffles of row j of the
+// Layout.  A group of threads runs one chain of fits (a fit_multik sweep
+// warm-starts each fit from the previous result, so a chain is sequential):
+// one warp when there are many chains, or the W = 4 warps of a CTA when there
+// are at most as many chains as SMs, so that the per-point work of a chain is
+// spread over the four sub-partitions of its SM (on GB300 an FP64 instruction
+// occupies a sub-partition's FP64 pipe for about 64 cycles whatever the
+// number of active lanes, and a single chain is bound by that latency).  The
+// n x n state (the triangular factor, the step, the trust region) is computed
+// by every thread of the group identically; the m data points are spread
+// over the threads (point i on thread i % (32 W)) and every sum over them is
+// an xor-butterfly reduction in each warp followed by the warp totals added in
+// warp order, which leaves the same bits in every thread.  The Jacobian
+// columns and the two residual vectors live in the group's slot of the
+// workspace; each element is only touched by the thread that owns its point,
+// so the only exchanges are the sums and the broadcast of row j of the
 // factor.  The number of varying parameters is a template argument, so the
 // small arrays stay in registers.
+//
+// Arithmetic against MINPACK's: the per-point divisions (by the difference
+// step in the Jacobian, by the column norm in the Householder step) are
+// multiplications by the reciprocal, and the sums over the points use fused
+// multiply-adds; with the different summation order these change results in
+// the last bits, as any other order of the same operations would.
 //
 // The files including this header are compiled without multiply-add
 // contraction (-fmad=false), as the host arithmetic they follow has none.
@@ -139,6 +151,71 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+constexpr int kMaxW = 4;  // warps of a group
+
+// The threads that run one chain: one warp (W = 1) or the W warps of a CTA.
+template <int W>
+struct Grp {
+  int tid;        // thread in the group
+  int lane, warp;
+  double* red;    // [2][kMaxW][kMaxP] per-warp totals (W > 1), two buffers used in turn
+  int* flags;     // [2][kMaxW]
+  double* bc;     // [2][kMaxP] values broadcast by one thread
+  int buf = 0;
+
+  __device__ void sync() {
+    if (W > 1) __syncthreads(); else __syncwarp();
+  }
+
+  // v[0..n-1] <- their sums over the group, flag <- OR over the group, and
+  // bv[0..nb-1] <- the values thread `owner` holds there (owner < 32 W).
+  // n, nb are compile-time after unrolling.  One barrier for W > 1: a buffer is
+  // written again two calls later, after every thread has read it.
+  template <int N, int NB>
+  __device__ void sum(double (&v)[N], int n, bool& flag, double (&bv)[NB], int nb, int owner) {
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      if (k < n) v[k] = warp_sum(v[k]);
+    const bool wflag = __any_sync(0xffffffffu, flag);
+    if (W == 1) {
+      flag = wflag;
+#pragma unroll
+      for (int k = 0; k < NB; ++k)
+        if (k < nb) bv[k] = __shfl_sync(0xffffffffu, bv[k], owner);
+      return;
+    }
+    double* r = red + buf * (kMaxW * kMaxP);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        if (k < n) r[warp * kMaxP + k] = v[k];
+      flags[buf * kMaxW + warp] = wflag;
+    }
+    if (tid == owner) {
+#pragma unroll
+      for (int k = 0; k < NB; ++k)
+        if (k < nb) bc[buf * kMaxP + k] = bv[k];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      if (k < n) {
+        double t = r[k];
+#pragma unroll
+        for (int q = 1; q < W; ++q) t += r[q * kMaxP + k];
+        v[k] = t;
+      }
+    bool f = false;
+#pragma unroll
+    for (int q = 0; q < W; ++q) f |= flags[buf * kMaxW + q] != 0;
+    flag = f;
+#pragma unroll
+    for (int k = 0; k < NB; ++k)
+      if (k < nb) bv[k] = bc[buf * kMaxP + k];
+    buf ^= 1;
+  }
+};
+
 // a[i] for a runtime index i over a register array (an unrolled select keeps a in registers)
 template <int N, class T>
 __device__ __forceinline__ T sel(const T (&a)[N], int i) {
@@ -195,11 +272,11 @@ struct Batch {
   int nslots;
 };
 
-// One fit.  NV: varying parameters.
-template <int NV>
+// One fit.  NV: varying parameters; W: warps of the group.
+template <int NV, int W>
 struct Fit {
   const Batch& b;
-  const int lane;
+  Grp<W>& G;
   const double* y;
   const double* w;
   double* fj[NV];
@@ -210,35 +287,47 @@ struct Fit {
   long long nfev = 0;
   int status = kOk;
 
-  __device__ Fit(const Batch& b_, int lane_) : b(b_), lane(lane_) {}
+  __device__ Fit(const Batch& b_, Grp<W>& g) : b(b_), G(g) {}
 
   __device__ void set_point(const double (&u)[NV]) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      const double v = from_internal(u[k], lo[k], hi[k], kind[k]);
+    for (int k = 0; k < NV; ++k) set_one(k, from_internal(u[k], lo[k], hi[k], kind[k]));
+  }
+
+  // external value of varying parameter k
+  __device__ void set_one(int k, double v) {
 #pragma unroll
-      for (int p = 0; p < kMaxP; ++p)
-        if (p == vix[k]) pe[p] = v;
-    }
+    for (int p = 0; p < kMaxP; ++p)
+      if (p == vix[k]) pe[p] = v;
+  }
+  __device__ double get_one(int k) const {
+    double v = 0.0;
+#pragma unroll
+    for (int p = 0; p < kMaxP; ++p)
+      if (p == vix[k]) v = pe[p];
+    return v;
   }
 
   // residuals (model - y) * w at the current pe into out; returns the sum of squares.
-  // With fd != 0, out[i] = (r_i - fv[i]) / fd (a Jacobian column) and the sum is over those.
-  __device__ double evaluate(double* out, const double* fv, double fd) {
+  // With rfd != 0, out[i] = (r_i - fv[i]) * rfd (a Jacobian column, rfd = 1 / step) and the
+  // sum is over those.
+  __device__ double evaluate(double* out, const double* fv, double rfd) {
     double s = 0.0;
     bool bad = false;
-    for (int i = lane; i < b.m; i += 32) {
+    for (int i = G.tid; i < b.m; i += 32 * W) {
       double r = model_eval(b.model, b.x[i], pe) - y[i];
       if (w) r = r * w[i];
       bad |= !isfinite(r);
-      if (fd != 0.0) r = (r - fv[i]) / fd;
+      if (rfd != 0.0) r = (r - fv[i]) * rfd;
       out[i] = r;
-      s += r * r;
+      s = __fma_rn(r, r, s);
     }
-    if (__any_sync(0xffffffffu, bad)) status = kNonFinite;
+    double v[1] = {s}, none[1];
+    G.sum(v, 1, bad, none, 0, -1);
+    if (bad) status = kNonFinite;
     ++nfev;
     if (nfev > b.max_nfev && status == kOk) status = kAborted;
-    return warp_sum(s);
+    return v[0];
   }
 };
 
@@ -246,10 +335,11 @@ struct Fit {
 // pivoting), each reflection also applied to wt (a copy of the residuals) as
 // it is formed.  colsq: squared column norms.  Outputs: R (upper triangle, by
 // pivot position), ipvt (position -> parameter), acnorm (by parameter), qtf.
-template <int NV>
-__device__ void qr_pivot(Fit<NV>& F, const double (&colsq)[NV], double* wt, double (&R)[NV][NV], int (&ipvt)[NV],
+template <int NV, int W>
+__device__ void qr_pivot(Fit<NV, W>& F, const double (&colsq)[NV], double* wt, double (&R)[NV][NV], int (&ipvt)[NV],
                          double (&acnorm)[NV], double (&qtf)[NV]) {
-  const int m = F.b.m, lane = F.lane;
+  const int m = F.b.m, tid = F.G.tid;
+  constexpr int S = 32 * W;
   double rdiag[NV], wa[NV];
   bool recomp[NV];
 #pragma unroll
@@ -264,29 +354,35 @@ __device__ void qr_pivot(Fit<NV>& F, const double (&colsq)[NV], double* wt, doub
   }
 #pragma unroll
   for (int j = 0; j < NV; ++j) {
-    // squared norms of the columns below row j-1, and row j (lane j owns point j)
+    // squared norms of the columns below row j-1, and row j with wt[j] from the thread owning point j
     double fresh[NV], rowj[NV];
-    if (j == 0) {
+    double part[NV], bv[NV + 1];
 #pragma unroll
-      for (int k = 0; k < NV; ++k) fresh[k] = colsq[k];
-    } else {
-      double part[NV];
-#pragma unroll
-      for (int k = 0; k < NV; ++k) part[k] = 0.0;
-      for (int i = lane; i < m; i += 32) {
+    for (int k = 0; k < NV; ++k) part[k] = 0.0;
+    if (j > 0)
+      for (int i = tid; i < m; i += S) {
         if (i < j) continue;
 #pragma unroll
         for (int k = j; k < NV; ++k) {
           const double v = F.fj[ipvt[k]][i];
-          part[k] += v * v;
+          part[k - j] = __fma_rn(v, v, part[k - j]);
         }
       }
 #pragma unroll
-      for (int k = 0; k < NV; ++k) fresh[k] = k >= j ? warp_sum(part[k]) : 0.0;
-    }
+    for (int k = 0; k <= NV; ++k) bv[k] = 0.0;
+    if (tid == j) {
 #pragma unroll
-    for (int k = j; k < NV; ++k) rowj[k] = __shfl_sync(0xffffffffu, lane == j ? F.fj[ipvt[k]][j] : 0.0, j);
-    const double wj = __shfl_sync(0xffffffffu, lane == j ? wt[j] : 0.0, j);
+      for (int k = j; k < NV; ++k) bv[k - j] = F.fj[ipvt[k]][j];
+      bv[NV - j] = wt[j];
+    }
+    bool nf = false;
+    F.G.sum(part, j > 0 ? NV - j : 0, nf, bv, NV - j + 1, j);
+#pragma unroll
+    for (int k = j; k < NV; ++k) {
+      fresh[k] = j > 0 ? part[k - j] : colsq[k];
+      rowj[k] = bv[k - j];
+    }
+    const double wj = bv[NV - j];
     // norms flagged at the previous step are taken afresh (MINPACK recomputes them there)
 #pragma unroll
     for (int k = j; k < NV; ++k)
@@ -316,40 +412,44 @@ __device__ void qr_pivot(Fit<NV>& F, const double (&colsq)[NV], double* wt, doub
     double ajnorm = sqrt(fresh[j]);
     if (ajnorm != 0.0) {
       if (rowj[j] < 0.0) ajnorm = -ajnorm;
-      const double vjj = rowj[j] / ajnorm + 1.0;
+      const double rn = 1.0 / ajnorm;
+      const double vjj = rowj[j] * rn + 1.0;
       double* cj = F.fj[ipvt[j]];
-      double dot[NV], dw = 0.0;
+      double dot[NV];  // dot[0]: with wt; dot[k - j]: with column k > j
 #pragma unroll
       for (int k = 0; k < NV; ++k) dot[k] = 0.0;
-      for (int i = lane; i < m; i += 32) {
+      for (int i = tid; i < m; i += S) {
         if (i < j) continue;
-        double v = cj[i] / ajnorm;
+        double v = cj[i] * rn;
         if (i == j) v = v + 1.0;
         cj[i] = v;
-        dw += v * wt[i];
+        dot[0] = __fma_rn(v, wt[i], dot[0]);
 #pragma unroll
-        for (int k = j + 1; k < NV; ++k) dot[k] += v * F.fj[ipvt[k]][i];
+        for (int k = j + 1; k < NV; ++k) dot[k - j] = __fma_rn(v, F.fj[ipvt[k]][i], dot[k - j]);
       }
-      const double tw = -warp_sum(dw) / vjj;
+      double none[1];
+      F.G.sum(dot, NV - j, nf, none, 0, -1);
+      const double rv = 1.0 / vjj;
+      const double tw = -dot[0] * rv;
       double tk[NV];
 #pragma unroll
-      for (int k = j + 1; k < NV; ++k) tk[k] = warp_sum(dot[k]) / vjj;
-      for (int i = lane; i < m; i += 32) {
+      for (int k = j + 1; k < NV; ++k) tk[k] = dot[k - j] * rv;
+      for (int i = tid; i < m; i += S) {
         if (i < j) continue;
         const double v = cj[i];
-        wt[i] = wt[i] + v * tw;
+        wt[i] = __fma_rn(v, tw, wt[i]);
 #pragma unroll
-        for (int k = j + 1; k < NV; ++k) F.fj[ipvt[k]][i] = F.fj[ipvt[k]][i] - tk[k] * v;
+        for (int k = j + 1; k < NV; ++k) F.fj[ipvt[k]][i] = __fma_rn(-tk[k], v, F.fj[ipvt[k]][i]);
       }
-      qtf[j] = wj + vjj * tw;
+      qtf[j] = __fma_rn(vjj, tw, wj);
 #pragma unroll
       for (int k = j + 1; k < NV; ++k) {
-        R[j][k] = rowj[k] - tk[k] * vjj;
+        R[j][k] = __fma_rn(-tk[k], vjj, rowj[k]);
         if (rdiag[k] != 0.0) {
           const double t = R[j][k] / rdiag[k];
           rdiag[k] *= sqrt(fmax(0.0, 1.0 - t * t));
-          const double q = rdiag[k] / wa[k];
-          if (0.05 * (q * q) <= kEpsMch) recomp[k] = true;
+          // 0.05 (rdiag / wa)^2 <= eps, without the division
+          if (0.05 * (rdiag[k] * rdiag[k]) <= kEpsMch * (wa[k] * wa[k])) recomp[k] = true;
         }
       }
     } else {
@@ -527,8 +627,8 @@ __device__ double lmpar(const double (&R)[NV][NV], const int (&ipvt)[NV], const 
 }
 
 // lmdif on one problem; u holds the internal starting point and receives the result.
-template <int NV>
-__device__ void lmdif(Fit<NV>& F, double (&u)[NV], double*& fv, double*& wt, double& fsq, int& info,
+template <int NV, int W>
+__device__ void lmdif(Fit<NV, W>& F, double (&u)[NV], double*& fv, double*& wt, double& fsq, int& info,
                       double (&R)[NV][NV], int (&ipvt)[NV]) {
   const Batch& b = F.b;
   const double eps = sqrt(fmax(b.epsfcn, kEpsMch));
@@ -540,20 +640,20 @@ __device__ void lmdif(Fit<NV>& F, double (&u)[NV], double*& fv, double*& wt, dou
   double par = 0.0, delta = 0.0, xnorm = 0.0;
   double diag[NV], acnorm[NV], qtf[NV];
   for (int iter = 1;;) {
-    // forward-difference Jacobian
+    // forward-difference Jacobian (only the perturbed parameter is mapped again)
     double colsq[NV];
 #pragma unroll
     for (int j = 0; j < NV; ++j) {
       const double t = u[j];
       double h = eps * fabs(t);
       if (h == 0.0) h = eps;
-      u[j] = t + h;
-      F.set_point(u);
-      colsq[j] = F.evaluate(F.fj[j], fv, h);
-      u[j] = t;
+      const double keep = F.get_one(j);
+      F.set_one(j, from_internal(t + h, F.lo[j], F.hi[j], F.kind[j]));
+      colsq[j] = F.evaluate(F.fj[j], fv, 1.0 / h);
+      F.set_one(j, keep);
       if (F.status != kOk) return;
     }
-    for (int i = F.lane; i < b.m; i += 32) wt[i] = fv[i];
+    for (int i = F.G.tid; i < b.m; i += 32 * W) wt[i] = fv[i];
     qr_pivot(F, colsq, wt, R, ipvt, acnorm, qtf);
     if (iter == 1) {
 #pragma unroll
@@ -568,13 +668,16 @@ __device__ void lmdif(Fit<NV>& F, double (&u)[NV], double*& fv, double*& wt, dou
     // scaled gradient
     double gnorm = 0.0;
     if (fnorm != 0.0) {
+      double qn[NV];
+#pragma unroll
+      for (int i = 0; i < NV; ++i) qn[i] = qtf[i] / fnorm;
 #pragma unroll
       for (int j = 0; j < NV; ++j) {
         const double an = sel(acnorm, ipvt[j]);
         if (an != 0.0) {
           double s = 0.0;
 #pragma unroll
-          for (int i = 0; i <= j; ++i) s += R[i][j] * (qtf[i] / fnorm);
+          for (int i = 0; i <= j; ++i) s += R[i][j] * qn[i];
           gnorm = fmax(gnorm, fabs(s / an));
         }
       }
@@ -652,8 +755,9 @@ __device__ void lmdif(Fit<NV>& F, double (&u)[NV], double*& fv, double*& wt, dou
   }
 }
 
-template <int NV>
-__device__ void run_problem(const Batch& b, int prob, double* slot, int lane) {
+template <int NV, int W>
+__device__ void run_problem(const Batch& b, int prob, double* slot, Grp<W>& G) {
+  const int lane = G.tid;
   const int32_t* pr = b.problems + 4 * (size_t)prob;
   const int yrow = pr[0], wrow = pr[1], pred = pr[2];
   const uint32_t vary = (uint32_t)pr[3];
@@ -671,10 +775,10 @@ __device__ void run_problem(const Batch& b, int prob, double* slot, int lane) {
       b.info[prob] = 0;
       b.status[prob] = kInvalid;
     }
-    __syncwarp();
+    G.sync();
     return;
   }
-  Fit<NV> F(b, lane);
+  Fit<NV, W> F(b, G);
   F.y = b.y + (size_t)yrow * b.ldy;
   F.w = wrow >= 0 ? b.w + (size_t)wrow * b.ldw : nullptr;
   double* fv = slot;
@@ -728,9 +832,10 @@ __device__ void run_problem(const Batch& b, int prob, double* slot, int lane) {
 #pragma unroll
       for (int k = 0; k < NV; ++k)
         if (k == l) g = scale_gradient(u[k], F.lo[k], F.hi[k], F.kind[k]);
+      const double rg = 1.0 / g;
 #pragma unroll
       for (int i = 0; i < NV; ++i) {
-        Rp[i][j] = i <= j ? R[i][j] / g : 0.0;
+        Rp[i][j] = i <= j ? R[i][j] * rg : 0.0;
         if (!isfinite(Rp[i][j])) cov = 1;
       }
       if (Rp[j][j] == 0.0) singular = true;
@@ -738,6 +843,9 @@ __device__ void run_problem(const Batch& b, int prob, double* slot, int lane) {
     if (cov == 0 && singular) cov = 2;
     if (cov == 0) {
       // Ui = Rp^{-1} (upper triangular, back substitution column by column)
+      double rd[NV];
+#pragma unroll
+      for (int i = 0; i < NV; ++i) rd[i] = 1.0 / Rp[i][i];
 #pragma unroll
       for (int c = 0; c < NV; ++c) {
 #pragma unroll
@@ -745,7 +853,7 @@ __device__ void run_problem(const Batch& b, int prob, double* slot, int lane) {
           double s = i == c ? 1.0 : 0.0;
 #pragma unroll
           for (int k = i + 1; k < NV; ++k) s -= Rp[i][k] * Ui[k][c];
-          Ui[i][c] = i <= c ? s / Rp[i][i] : 0.0;
+          Ui[i][c] = i <= c ? s * rd[i] : 0.0;
         }
       }
       const int nfree = b.m - NV;
@@ -782,22 +890,33 @@ __device__ void run_problem(const Batch& b, int prob, double* slot, int lane) {
     b.status[prob] = F.status;
   }
   if (b.residual)
-    for (int i = lane; i < b.m; i += 32) b.residual[(size_t)prob * b.m + i] = fv[i];
-  __syncwarp();
+    for (int i = G.tid; i < b.m; i += 32 * W) b.residual[(size_t)prob * b.m + i] = fv[i];
+  G.sync();
 }
 
-template <int NV>
+// W = 1: each warp of the CTA runs its own chains; W = 4: the CTA runs one chain at a time.
+template <int NV, int W>
 __global__ void __launch_bounds__(32 * kWarpsPerCta) k_fit_lm(Batch b) {
-  const int lane = threadIdx.x & 31;
-  const int gw = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
-  if (gw >= b.nslots) return;
-  double* slot = b.ws + (size_t)gw * b.slot_doubles;
-  for (int c = gw; c < b.nchains; c += b.nslots) {
+  static_assert(W == 1 || W == kWarpsPerCta, "a group is one warp or the whole CTA");
+  __shared__ double red[2 * kMaxW * kMaxP];
+  __shared__ int flags[2 * kMaxW];
+  __shared__ double bc[2 * kMaxP];
+  Grp<W> G;
+  G.lane = threadIdx.x & 31;
+  G.warp = threadIdx.x >> 5;
+  G.tid = W > 1 ? (int)threadIdx.x : G.lane;
+  G.red = red;
+  G.flags = flags;
+  G.bc = bc;
+  const int gid = W > 1 ? (int)blockIdx.x : (int)(blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5));
+  if (gid >= b.nslots) return;  // whole groups leave together
+  double* slot = b.ws + (size_t)gid * b.slot_doubles;
+  for (int c = gid; c < b.nchains; c += b.nslots) {
     bool stop = false;
     for (int e = b.chain_off[c]; e < b.chain_off[c + 1] && !stop; ++e) {
       const int prob = b.chain_list[e];
       if (prob < 0 || prob >= b.nprob) break;  // not a problem: the chain ends
-      run_problem<NV>(b, prob, slot, lane);
+      run_problem<NV, W>(b, prob, slot, G);
       // a fit that raised in the reference ends its sweep there
       stop = b.status[prob] == kNonFinite || b.status[prob] == kInvalid;
     }
@@ -805,19 +924,22 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_fit_lm(Batch b) {
 }
 
 template <int NV>
-cudaError_t launch(const Batch& b, unsigned grid, cudaStream_t st) {
-  k_fit_lm<NV><<<grid, 32 * kWarpsPerCta, 0, st>>>(b);
+cudaError_t launch(const Batch& b, unsigned grid, int group_warps, cudaStream_t st) {
+  if (group_warps > 1)
+    k_fit_lm<NV, kWarpsPerCta><<<grid, 32 * kWarpsPerCta, 0, st>>>(b);
+  else
+    k_fit_lm<NV, 1><<<grid, 32 * kWarpsPerCta, 0, st>>>(b);
   return cudaGetLastError();
 }
 
 // one launcher per number of varying parameters, each in its own translation unit
-cudaError_t launch_nv1(const Batch& b, unsigned grid, cudaStream_t st);
-cudaError_t launch_nv2(const Batch& b, unsigned grid, cudaStream_t st);
-cudaError_t launch_nv3(const Batch& b, unsigned grid, cudaStream_t st);
-cudaError_t launch_nv4(const Batch& b, unsigned grid, cudaStream_t st);
-cudaError_t launch_nv5(const Batch& b, unsigned grid, cudaStream_t st);
-cudaError_t launch_nv6(const Batch& b, unsigned grid, cudaStream_t st);
-cudaError_t launch_nv7(const Batch& b, unsigned grid, cudaStream_t st);
+cudaError_t launch_nv1(const Batch& b, unsigned grid, int group_warps, cudaStream_t st);
+cudaError_t launch_nv2(const Batch& b, unsigned grid, int group_warps, cudaStream_t st);
+cudaError_t launch_nv3(const Batch& b, unsigned grid, int group_warps, cudaStream_t st);
+cudaError_t launch_nv4(const Batch& b, unsigned grid, int group_warps, cudaStream_t st);
+cudaError_t launch_nv5(const Batch& b, unsigned grid, int group_warps, cudaStream_t st);
+cudaError_t launch_nv6(const Batch& b, unsigned grid, int group_warps, cudaStream_t st);
+cudaError_t launch_nv7(const Batch& b, unsigned grid, int group_warps, cudaStream_t st);
 
 }  // namespace fitlm
 }  // namespace fddm

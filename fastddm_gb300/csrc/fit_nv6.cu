@@ -3,6 +3,8 @@
 
 namespace fddm {
 namespace fitlm {
-cudaError_t launch_nv6(const Batch& b, unsigned grid, cudaStream_t st) { return launch<6>(b, grid, st); }
+cudaError_t launch_nv6(const Batch& b, unsigned grid, int group_warps, cudaStream_t st) {
+  return launch<6>(b, grid, group_warps, st);
+}
 }  // namespace fitlm
 }  // namespace fddm

@@ -80,6 +80,9 @@ def fit(model: Model, xdata: np.ndarray, ydata: np.ndarray, params: Optional[Uni
 
     ``fitargs`` go to :meth:`Model.fit` (``weights``, ``fit_kws``, ``max_nfev``, ``gpu_id``...).
     """
+    from .fit_models import from_lmfit
+
+    model = from_lmfit(model)
     model_params = model.make_params()
     fitargs[model.independent_vars[0]] = xdata
     if estimate_simple_parameters:
@@ -168,6 +171,9 @@ def fit_multik(data: Union[AzimuthalAverage, IntermediateScatteringFunction], mo
         raise NotImplementedError("fixed_params_expr: parameter expressions are not supported by the device fits")
     if warm_start not in ("chain", "ref", "none"):
         raise ValueError("warm_start must be 'chain', 'ref' or 'none'")
+    from .fit_models import from_lmfit
+
+    model = from_lmfit(model)
     model_params = model.make_params()
     ref_params = _copy(ref_params)
     fixed_params, fixed_params_min, fixed_params_max = (_copy(fixed_params), _copy(fixed_params_min),
@@ -177,7 +183,7 @@ def fit_multik(data: Union[AzimuthalAverage, IntermediateScatteringFunction], mo
     Y = np.asarray(data.data, dtype=np.float64)
     K = len(data.k)
     if ref_params is not None:
-        model_params.update(ref_params)
+        model_params.update(ref_params)  # lmfit Parameters are converted
     for p in names:
         if p in fitargs:
             model_params[p].value = fitargs.pop(p)

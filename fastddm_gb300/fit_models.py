@@ -111,3 +111,32 @@ flory_schulz_model = _model(_flory_schulz, FLORY_SCHULZ_SF,
                             {"A": _POS, "B": _NOISE, "Gamma": _POS, "sigma": dict(value=1.0, min=EPSILON, max=1.0)})
 exponential_distribution_model = _model(_flory_schulz, FLORY_SCHULZ_SF,
                                         {"A": _POS, "B": _NOISE, "Gamma": _POS, "sigma": dict(value=1.0, vary=False)})
+
+
+# the device evaluation of each model function of the reference, by the function's name
+_DEVICE_IDS = {
+    "_generic_exponential_isf": GENERIC_EXP_ISF, "_double_exponential_isf": DOUBLE_EXP_ISF,
+    "_flory_schulz_isf": FLORY_SCHULZ_ISF, "_generic_exponential": GENERIC_EXP_SF,
+    "_double_exponential": DOUBLE_EXP_SF, "_flory_schulz": FLORY_SCHULZ_SF, "_simple_exp": SIMPLE_EXP,
+    "_simple_image_structure_function": SIMPLE_SF,
+}
+
+
+def from_lmfit(model) -> Model:
+    """The device model for an lmfit ``Model`` built on one of the reference's
+    functions (``fit_models.py``, ``fit.py``), with its parameter hints.
+
+    Raises ``NotImplementedError`` for any other function: only these models
+    have a device evaluation.
+    """
+    if isinstance(model, Model):
+        return model
+    func = getattr(model, "func", None)
+    name = getattr(func, "__name__", None)
+    if name not in _DEVICE_IDS:
+        raise NotImplementedError(f"no device evaluation for the model function {name!r}")
+    m = Model(func, _DEVICE_IDS[name])
+    for pname, hint in (getattr(model, "param_hints", None) or {}).items():
+        if pname in m.param_names:
+            m.set_param_hint(pname, **{k: v for k, v in hint.items() if k in ("value", "vary", "min", "max", "expr")})
+    return m

@@ -254,3 +254,34 @@ def test_simple_parameter_helper():
     p = gfit._simple_structure_function_parameter_helper(x, y)
     assert abs(p["B"].value - 3.0) < 0.5 and abs(p["A"].value - 50.0) < 1.0
     assert 1.0 < p["tau"].value < 2.0
+
+
+def test_lmfit_models_and_parameters_are_converted(monkeypatch):
+    """A reference user's lmfit objects (duck-typed here: lmfit is not installed) drive the device fits."""
+
+    class LmParam:
+        def __init__(self, name, value, vary=True, min=-np.inf, max=np.inf, expr=None):
+            self.name, self.value, self.vary, self.min, self.max, self.expr = name, value, vary, min, max, expr
+            self.stderr = None
+
+    class LmModel:  # what lmfit.Model(_generic_exponential) with set_param_hint calls holds
+        def __init__(self, func):
+            self.func = func
+            self.param_hints = {}
+
+    m = LmModel(fit_models._generic_exponential)
+    m.param_hints = {"A": {"value": 1.0, "min": EPS, "max": np.inf}, "B": {"value": 0.0},
+                     "Gamma": {"value": 1.0, "min": EPS, "max": np.inf}, "beta": {"value": 1.0, "vary": False}}
+    dm = fit_models.from_lmfit(m)
+    assert dm.device_id == fit_models.GENERIC_EXP_SF and dm.param_names == ["A", "B", "Gamma", "beta"]
+    p = dm.make_params()
+    assert p["beta"].vary is False and p["A"].min == EPS
+    p.update({"A": LmParam("A", 7.0, min=1.0)})
+    assert isinstance(p["A"], _fitting.Parameter) and p["A"].value == 7.0 and p["A"].min == 1.0
+    with pytest.raises(NotImplementedError):
+        fit_models.from_lmfit(LmModel(lambda x, a: a * x))
+    aa, (A, B, G) = synthetic_aa(K=8, seed=4)
+    monkeypatch.setattr(gfit, "run_fits", FakeDevice("simple_exponential_model"))
+    ref_params = {"A": LmParam("A", A[3], min=EPS), "B": LmParam("B", B[3]), "Gamma": LmParam("Gamma", G[3], min=EPS)}
+    table, _ = gfit.fit_multik(aa, m, 3, ref_params=ref_params)
+    np.testing.assert_allclose(table["Gamma"], G, rtol=0.05)

@@ -8,10 +8,14 @@ different paths to the same minimum.  On curves started within a factor of
 about two of the solution the fitted parameters agree to 1e-5 of their scale
 (the amplitude for B) or a tenth of their standard error, whichever is
 larger (MINPACK's xtol test stops a poorly determined parameter early, at a
-point that depends on the path), chi^2 to 1e-9 relative, standard errors to
-2e-2 relative (they come from the last Jacobian, which MINPACK evaluates at
+point that depends on the path), chi^2 to 1e-9 relative or 0.05 of a
+reduced chi-square unit (a one-standard-error change of any parameter moves
+chi^2 by about one such unit; where xtol stops a run in a flat valley the
+two runs' chi^2 differ by less than that), standard errors to
+5e-2 relative (they come from the last Jacobian, which MINPACK evaluates at
 the iterate before the final step, so a run that stops one step apart reads
-a slightly different one), and the success flags exactly.
+a slightly different one; started at the solution, where both runs read the
+same Jacobian, they agree to 1e-4), and the success flags exactly.
 """
 
 import numpy as np
@@ -23,8 +27,9 @@ pytestmark = pytest.mark.gpu
 
 PAR_TOL = 1e-5   # of the parameter's scale, or
 SE_FRAC = 0.1    # of its standard error, whichever is larger
-CHI_TOL = 1e-9
-SE_TOL = 2e-2
+CHI_TOL = 1e-9   # relative, or
+CHI_RED = 0.05   # of a reduced chi-square unit, whichever is larger
+SE_TOL = 5e-2
 
 # model name -> (true parameters, starting values)
 CASES = {
@@ -98,7 +103,8 @@ def _compare(name, dev, ora, names):
             assert abs(ds / os_ - 1) < SE_TOL, (name, p, ds, os_)
         else:
             assert ds == 0.0
-    assert abs(dev.chisqr / ora["chisqr"] - 1) < CHI_TOL, (name, dev.chisqr, ora["chisqr"])
+    tol = max(CHI_TOL * ora["chisqr"], CHI_RED * ora["redchi"])
+    assert abs(dev.chisqr - ora["chisqr"]) <= tol, (name, dev.chisqr, ora["chisqr"], tol)
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
@@ -119,6 +125,30 @@ def test_model_fit_matches_the_oracle(name):
         _compare(name, dev, ora, names)
         # residual and best fit as lmfit reports them
         np.testing.assert_allclose(dev.residual, (dev.best_fit - y) * w, rtol=1e-9, atol=1e-9 * np.abs(w * y).max())
+
+
+@pytest.mark.parametrize("name", ["simple_exponential_model", "stretched_exponential_isf_model",
+                                  "double_exponential_model", "flory_schulz_model"])
+def test_standard_errors_at_the_solution(name):
+    """Started at the oracle's solution both runs factor the same Jacobian: lmfit's covariance
+    (inv(R^T R) through the bound mappings, times chi^2 / nfree) agrees closely."""
+    model = _model(name)
+    func, names, _ = fo.MODELS[name]
+    _, start = CASES[name]
+    x, y = _curve(name, 11)
+    op = fo.make_params(name)
+    for k, v in start.items():
+        op[k]["value"] = v
+    first = fo.lm_fit(func, names, op, x, y)
+    for k in names:
+        op[k]["value"] = first["values"][k]
+    ora = fo.lm_fit(func, names, op, x, y)
+    params = model.make_params(**{k: first["values"][k] for k in names})
+    dev = model.fit(y, params=params, **{model.independent_vars[0]: x})
+    for p in names:
+        os_, ds = ora["stderr"][p], dev.params[p].stderr
+        if os_ is not None and np.isfinite(os_) and os_ > 0:
+            assert abs(ds / os_ - 1) < 1e-4, (name, p, ds, os_)
 
 
 def test_fit_with_estimated_simple_parameters():
