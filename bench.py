@@ -255,6 +255,129 @@ def azavg_record(out, nx: int, ny: int, device, bins: int = 512, reps: int = 3) 
     return rec, aa.AzimuthalAverage(avg.cpu().numpy(), err.cpu().numpy(), setup.k, None, setup.bin_edges)
 
 
+def device_azavg(out, nx: int, ny: int, device, bins: int):
+    """The azimuthal average of a structure function in device memory (``bins`` bins over
+    (0, ky[-1]), the exact order), as an AzimuthalAverage with tau unset."""
+    from fastddm_gb300 import azimuthalaverage as aa
+
+    kx = 2 * np.pi * np.fft.fftfreq(nx)[: nx // 2 + 1]
+    ky = 2 * np.pi * np.fft.fftshift(np.fft.fftfreq(ny))
+    counts = np.full((ny, nx // 2 + 1), 2)
+    counts[:, 0] = 1
+    counts[:, -1] = 1 if nx % 2 == 0 else 2
+    gx, gy = np.meshgrid(kx, ky)
+    setup = aa.bin_setup(np.sqrt(gx ** 2 + gy ** 2), bins, (0, ky[-1]), None, None, counts, True)
+    avg, err = aa._run_device(out, setup, True, device, True, host=True)
+    return aa.AzimuthalAverage(avg, err, setup.k, None, setup.bin_edges)
+
+
+def batch_fit_record(jobs, device, sample: int = 4) -> dict:
+    """The fits of config 4's pipeline: each stack's azimuthal average (height / 4 bins) and one
+    fit_multik_batch over all stacks (the reference's sweep for each, every sweep concurrent), against
+    the oracle's sweeps on the first ``sample`` stacks (one host core; extrapolated to all stacks by
+    their number of fits).  Set-up as in fit_record."""
+    import torch
+
+    from fastddm_gb300 import fit as gfit
+    from fastddm_gb300 import fit_models
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import fit_oracle as fo
+
+    setups = []
+    for j in jobs:
+        av = device_azavg(j.out, j.nx, j.ny, device, max(8, j.shape[1] // 4))
+        setups.append(fit_start(av, np.asarray(j.lags, dtype=np.float64), ref_frac=0.25))
+    model = fit_models.simple_exponential_model
+    bjobs = [dict(data=a, ref=ref, **kw) for a, ref, kw in setups]
+    best, best_tot = float("inf"), float("inf")
+    for _ in range(2):
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        res = gfit.fit_multik_batch(bjobs, model)
+        best_tot = min(best_tot, 1000 * (time.perf_counter() - t0))
+        best = min(best, res[0][0].device_ms)
+    nfits = [int(np.sum(~np.isnan(a.data[:, 0]))) + 1 for a, _, _ in setups]
+    func, names, _ = fo.MODELS["simple_exponential_model"]
+    t0 = time.perf_counter()
+    par = []
+    for (a, ref, kw), (tab, _) in list(zip(setups, res))[:sample]:
+        params = fo.make_params("simple_exponential_model")
+        for n in ("A", "B", "Gamma"):
+            params[n]["value"] = float(kw[n])
+        want = fo.fit_multik(func, names, params, a.tau, a.data, ref, err=a.err, use_err=True)
+        par.append(fit_parity(tab, want, a, func))
+    sample_ms = 1000 * (time.perf_counter() - t0)
+    oracle_all = sample_ms * sum(nfits) / sum(nfits[:sample])
+    return {"model": "simple_exponential_model", "stacks": len(jobs), "fits": int(sum(nfits)),
+            "lags_range": [min(a.tau.size for a, _, _ in setups), max(a.tau.size for a, _, _ in setups)],
+            "batch_device_ms": best, "batch_total_ms": best_tot,
+            "success": int(sum(int(np.sum(t["success"])) for t, _ in res)),
+            "oracle_sample_stacks": sample, "oracle_sample_ms": sample_ms,
+            "oracle_all_ms_extrapolated": oracle_all, "oracle_cores": 1,
+            "batch_vs_oracle": oracle_all / best,
+            "parity_sample": {"k_well_determined": sum(p["k_well_determined"] for p in par),
+                              "parity_max_over_tol": max(p["parity_max_over_tol"] for p in par),
+                              "chi2_equal": sum(p["chi2_equal"] for p in par),
+                              "chi2_device_lower": sum(p["chi2_device_lower"] for p in par),
+                              "chi2_device_higher": sum(p["chi2_device_higher"] for p in par),
+                              "success_agree": all(p["success_agree"] for p in par)}}
+
+
+def fit_start(azavg, tau: np.ndarray, ref_frac: float = 0.125):
+    """An azimuthal average set up for fit_multik as the reference's fit.py docstring does.
+
+    Bins whose error is 0 or not finite (the k = 0 bin holds one pixel) become
+    NaN rows; B from the "polyfit" noise estimate, A = 2 var - B and Gamma from
+    the half-decay lag at the reference k.  Returns (data, ref, keyword arguments).
+    """
+    import copy as _copy
+
+    from fastddm_gb300 import noise_est
+
+    a = _copy.copy(azavg)
+    a.tau = np.asarray(tau, dtype=np.float64)
+    data = a._data.copy()
+    bad = ~np.all(np.isfinite(a.err) & (a.err > 0), axis=1)
+    data[bad, 0] = np.nan
+    a._data = data
+    B_est, _ = noise_est.estimate_camera_noise(a, mode="polyfit")
+    valid = np.flatnonzero(~np.isnan(a.data[:, 0]))
+    ref = int(valid[int(len(valid) * ref_frac)])
+    A0 = 2.0 * a.var[ref] - B_est[ref]
+    half = np.abs((a.data[ref] - B_est[ref]) / A0 - 0.5)
+    G0 = 1.0 / a.tau[int(np.argmin(half))]
+    return a, ref, dict(A=A0, B=B_est[ref], Gamma=G0, use_err=True)
+
+
+def fit_parity(got, want, a, func) -> dict:
+    """Device sweep against the oracle's: parameters on the k the oracle determines well (converged,
+    A and Gamma to 10 %), over max(1e-5 of the scale, 0.1 standard error); chi^2 on every k, within
+    max(1e-9 relative, 0.05 reduced chi^2)."""
+    ok = ~np.isnan(want["A"])
+    with np.errstate(invalid="ignore", divide="ignore"):
+        rel = np.maximum(want["A_stderr"] / np.abs(want["A"]), want["Gamma_stderr"] / np.abs(want["Gamma"]))
+    wd = ok & want["success"] & np.isfinite(rel) & (rel < 0.1)
+    worst = 0.0
+    for n in ("A", "B", "Gamma"):
+        scale = np.abs(want["A"][wd]) if n == "B" else np.abs(want[n][wd])
+        tol = np.maximum(1e-5 * scale, 0.1 * want[f"{n}_stderr"][wd])
+        if wd.any():
+            worst = max(worst, float(np.max(np.abs(got[n][wd] - want[n][wd]) / tol)))
+    w = 1.0 / a.err
+    with np.errstate(invalid="ignore", over="ignore"):
+        chi_d = np.sum(((func(a.tau[None, :], got["A"][:, None], got["B"][:, None], got["Gamma"][:, None], 1.0)
+                         - a.data) * w) ** 2, axis=1)
+        chi_o = np.sum(((func(a.tau[None, :], want["A"][:, None], want["B"][:, None], want["Gamma"][:, None], 1.0)
+                         - a.data) * w) ** 2, axis=1)
+    ctol = np.maximum(1e-9 * chi_o, 0.05 * chi_o / (a.tau.size - 3))
+    return {"k": int(ok.sum()), "k_well_determined": int(wd.sum()), "parity_max_over_tol": worst,
+            "chi2_equal": int(np.sum(ok & (np.abs(chi_d - chi_o) <= ctol))),
+            "chi2_device_lower": int(np.sum(ok & (chi_o - chi_d > ctol))),
+            "chi2_device_higher": int(np.sum(ok & (chi_d - chi_o > ctol))),
+            "success_agree": bool(np.array_equal(got["success"], want["success"]))}
+
+
 def fit_record(azavg, tau: np.ndarray, reps: int = 3) -> dict:
     """fit_multik of the azimuthal average, as the reference's fit.py docstring sets it up.
 
@@ -270,30 +393,15 @@ def fit_record(azavg, tau: np.ndarray, reps: int = 3) -> dict:
     k, how many chi^2 agree within max(1e-9 relative, 0.05 reduced chi^2) and
     how many are lower or higher on the device.
     """
-    import copy as _copy
-
     from fastddm_gb300 import fit as gfit
-    from fastddm_gb300 import fit_models, noise_est
+    from fastddm_gb300 import fit_models
 
     sys.path.insert(0, str(ROOT / "oracle"))
     import fit_oracle as fo
 
-    a = _copy.copy(azavg)
-    a.tau = np.asarray(tau, dtype=np.float64)
-    data = a._data.copy()
-    bad = ~np.all(np.isfinite(a.err) & (a.err > 0), axis=1)
-    data[bad, 0] = np.nan
-    a._data = data
-    B_est, _ = noise_est.estimate_camera_noise(a, mode="polyfit")
-    valid = np.flatnonzero(~np.isnan(a.data[:, 0]))
-    ref = int(valid[len(valid) // 8])
-    A0 = 2.0 * a.var[ref] - B_est[ref]
-    half = np.abs((a.data[ref] - B_est[ref]) / A0 - 0.5)
-    G0 = 1.0 / a.tau[int(np.argmin(half))]
+    a, ref, kw = fit_start(azavg, tau)
     model = fit_models.simple_exponential_model
-    kw = dict(A=A0, B=B_est[ref], Gamma=G0, use_err=True)
-    rec = {"model": "simple_exponential_model", "k": int(valid.size), "lags": int(a.tau.size), "ref": ref,
-           "use_err": True}
+    rec = {"model": "simple_exponential_model", "lags": int(a.tau.size), "ref": ref, "use_err": True}
     tables = {}
     for order in ("chain", "ref"):
         best_dev, best_tot = float("inf"), float("inf")
@@ -314,32 +422,7 @@ def fit_record(azavg, tau: np.ndarray, reps: int = 3) -> dict:
     want = fo.fit_multik(func, names, params, a.tau, a.data, ref, err=a.err, use_err=True)
     rec["oracle_chain_ms"] = 1000 * (time.perf_counter() - t0)
     rec["oracle_cores"] = 1
-    got = tables["chain"]
-    ok = ~np.isnan(want["A"])
-    # parameters: on the k the oracle determines well (converged, every varying parameter to 10%)
-    with np.errstate(invalid="ignore", divide="ignore"):
-        rel = np.maximum(want["A_stderr"] / np.abs(want["A"]), want["Gamma_stderr"] / np.abs(want["Gamma"]))
-    wd = ok & want["success"] & np.isfinite(rel) & (rel < 0.1)
-    worst = 0.0
-    for n in ("A", "B", "Gamma"):
-        scale = np.abs(want["A"][wd]) if n == "B" else np.abs(want[n][wd])
-        tol = np.maximum(1e-5 * scale, 0.1 * want[f"{n}_stderr"][wd])
-        if wd.any():
-            worst = max(worst, float(np.max(np.abs(got[n][wd] - want[n][wd]) / tol)))
-    rec["k_well_determined"] = int(wd.sum())
-    rec["parity_max_over_tol"] = worst
-    # chi^2 on every fitted k; elsewhere (only A + B determined: the decay is faster than the first lag
-    # or slower than the last) each run stops at its own point of a flat valley
-    w = 1.0 / a.err
-    chi_d = np.sum(((func(a.tau[None, :], got["A"][:, None], got["B"][:, None], got["Gamma"][:, None], 1.0)
-                     - a.data) * w) ** 2, axis=1)
-    chi_o = np.sum(((func(a.tau[None, :], want["A"][:, None], want["B"][:, None], want["Gamma"][:, None], 1.0)
-                     - a.data) * w) ** 2, axis=1)
-    ctol = np.maximum(1e-9 * chi_o, 0.05 * chi_o / (a.tau.size - 3))
-    rec["chi2_equal"] = int(np.sum(ok & (np.abs(chi_d - chi_o) <= ctol)))
-    rec["chi2_device_lower"] = int(np.sum(ok & (chi_o - chi_d > ctol)))
-    rec["chi2_device_higher"] = int(np.sum(ok & (chi_d - chi_o > ctol)))
-    rec["success_agree"] = bool(np.array_equal(got["success"], want["success"]))
+    rec.update(fit_parity(tables["chain"], want, a, func))
     rec["chain_vs_oracle"] = rec["oracle_chain_ms"] / rec["chain_device_ms"]
     return rec
 
@@ -853,6 +936,10 @@ def run_batch(args):
     seq_ms = min(seq)
     identical = all(bool(torch.equal(a, j.out)) for a, j in zip(batch_out, jobs))
     del plans, batch_out
+    try:
+        fits = batch_fit_record(jobs, device)
+    except (ValueError, RuntimeError) as e:  # recorded, not fatal to the batch line
+        fits = {"error": f"{type(e).__name__}: {e}"}
     line = {
         "metric": "DDM frames/s (batched uneven stacks)", "value": value, "unit": "frames/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -865,7 +952,7 @@ def run_batch(args):
                           "how": "the same jobs through per-stack plans built before timing, back to back on one "
                                  "stream without host syncs (best of up to 3 passes)"},
         "batch_over_one_at_a_time": seq_ms / ms, "results_identical_to_one_at_a_time": identical,
-        "graph": "CUDA graph of fddm_b200_batch_launch, replayed each step",
+        "graph": "CUDA graph of fddm_b200_batch_launch, replayed each step", "fit_multik_batch": fits,
         "clocks": _clock_block(clk), "gpu_launches": launches,
     }
     print(json.dumps(line))

@@ -195,15 +195,17 @@ def check_bounds(lo: np.ndarray, hi: np.ndarray, names: Sequence[str]):
     return lo, hi
 
 
-def run_fits(model: "Model", x: np.ndarray, Y: np.ndarray, W: Optional[np.ndarray], problems: np.ndarray,
+def run_fits(model: "Model", X: np.ndarray, Y: np.ndarray, W: Optional[np.ndarray], problems: np.ndarray,
              stages: Sequence[Sequence[Sequence[int]]], init: np.ndarray, lo: np.ndarray, hi: np.ndarray,
              options: np.ndarray, gpu_id: int = 0, residual: bool = False) -> Dict[str, np.ndarray]:
     """Run the fits on the device.
 
-    problems: int32 (P, 4) rows (y row, weight row or -1, pred or -1, vary mask);
-    stages: launches in order, each a list of chains (lists of problem indices);
-    init, lo, hi: (P, nparams) starting values and bounds.  The result holds the
-    library's outputs and ``device_ms``, the time of the launches on the device.
+    X, Y, W: rows of abscissae, data and weights (W may be None), as wide as
+    the longest problem; problems: int32 (P, 6) rows (y row, weight row or -1,
+    pred or -1, vary mask, x row, number of points); stages: launches in order,
+    each a list of chains (lists of problem indices); init, lo, hi: (P, nparams)
+    starting values and bounds.  The result holds the library's outputs and
+    ``device_ms``, the time of the launches on the device.
     """
     lib = _lib.load()
     dev = _device(gpu_id)
@@ -213,16 +215,18 @@ def run_fits(model: "Model", x: np.ndarray, Y: np.ndarray, W: Optional[np.ndarra
     if len(nvs) != 1:
         raise ValueError("all fits of one call must vary the same number of parameters")
     nvary = nvs.pop()
-    m = int(x.shape[0])
-    if m < nvary:
-        raise TypeError(f"Improper input: func (m={m}) must be >= n={nvary}")
+    X = np.atleast_2d(X)
+    m = int(X.shape[1])
+    small = int(problems[:, 5].min())
+    if small < nvary:
+        raise TypeError(f"Improper input: func (m={small}) must be >= n={nvary}")
     f64 = dict(dtype=torch.float64, device=dev)
     i32 = dict(dtype=torch.int32, device=dev)
 
     def up(a, kind):
         return torch.as_tensor(np.array(a, dtype=np.float64 if kind is f64 else np.int32, order="C"), **kind)
 
-    dx, dy = up(x, f64), up(Y, f64)
+    dx, dy = up(X, f64), up(Y, f64)
     dw = None if W is None else up(W, f64)
     dprob, dinit, dlo, dhi = up(problems, i32), up(init, f64), up(lo, f64), up(hi, f64)
     vals = torch.empty((P, npar), **f64)
@@ -249,7 +253,7 @@ def run_fits(model: "Model", x: np.ndarray, Y: np.ndarray, W: Optional[np.ndarra
         t0.record(stream)
         for doff, dlist, nch in chain_tabs:
             _lib.check(lib.fddm_b200_fit_lm(
-                model.device_id, m, dx.data_ptr(), dy.data_ptr(), dy.shape[1], dy.shape[0],
+                model.device_id, m, dx.data_ptr(), dx.shape[1], dx.shape[0], dy.data_ptr(), dy.shape[1], dy.shape[0],
                 None if dw is None else dw.data_ptr(), 0 if dw is None else dw.shape[1],
                 0 if dw is None else dw.shape[0],
                 dprob.data_ptr(), P, doff.data_ptr(), dlist.data_ptr(), nch, nvary,
@@ -450,8 +454,8 @@ class Model:
         if weights is not None:
             W = np.broadcast_to(np.asarray(weights, dtype=np.float64), y.shape)[None, :]
         spec = FitSpec(self, params)
-        problems = np.array([[0, 0 if W is not None else -1, -1, spec.vary]], dtype=np.int32)
-        out = run_fits(self, x, y[None, :], W, problems, [[[0]]], spec.init[None], spec.lo[None], spec.hi[None],
+        problems = np.array([[0, 0 if W is not None else -1, -1, spec.vary, 0, y.size]], dtype=np.int32)
+        out = run_fits(self, x[None, :], y[None, :], W, problems, [[[0]]], spec.init[None], spec.lo[None], spec.hi[None],
                        lsq_options(fit_kws, max_nfev), gpu_id, residual=True)
         if int(out["status"][0]) == ST_NONFINITE:
             raise ValueError(NAN_MESSAGE)

@@ -20,9 +20,10 @@ int sm_count() {
   return nsm > 0 ? nsm : 152;
 }
 
-// Warps per chain: with at most one chain per SM a chain takes a whole CTA (its per-point work
-// spread over the SM's four sub-partitions); with more, each warp runs its own chains.
-int group_warps(uint64_t nchains) { return nchains <= (uint64_t)sm_count() ? fddm::fitlm::kWarpsPerCta : 1; }
+// Warps per chain: with at most two chains per SM a chain takes a whole CTA (its per-point work
+// spread over the SM's four sub-partitions, which one warp per chain would mostly leave idle); with
+// more, each warp runs its own chains (no sub-partition repeats the small-matrix work of another).
+int group_warps(uint64_t nchains) { return nchains <= 2 * (uint64_t)sm_count() ? fddm::fitlm::kWarpsPerCta : 1; }
 
 // groups resident at once (8 CTAs per SM)
 uint64_t max_slots(int group) { return (uint64_t)sm_count() * 8 * (fddm::fitlm::kWarpsPerCta / group); }
@@ -43,9 +44,9 @@ extern "C" int fddm_b200_fit_workspace_bytes(int model, uint64_t m, uint64_t nch
   return FDDM_OK;
 }
 
-extern "C" int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, const double* d_y, uint64_t ldy,
-                                uint64_t ny, const double* d_w, uint64_t ldw, uint64_t nw,
-                                const int32_t* d_problems, uint64_t nproblems,
+extern "C" int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, uint64_t ldx, uint64_t nx,
+                                const double* d_y, uint64_t ldy, uint64_t ny, const double* d_w, uint64_t ldw,
+                                uint64_t nw, const int32_t* d_problems, uint64_t nproblems,
                                 const int32_t* d_chain_offsets, const int32_t* d_chain_problems, uint64_t nchains,
                                 int nvary, const double* d_init, const double* d_min, const double* d_max,
                                 const double* options, double* d_values, double* d_stderr, double* d_chisqr,
@@ -56,15 +57,16 @@ extern "C" int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, const 
   if (np == 0) return fail_with(FDDM_ERR_INVALID, "unknown fit model");
   if (nvary < 1 || nvary > np) return fail_with(FDDM_ERR_INVALID, "nvary must be in 1..nparams");
   if ((uint64_t)nvary > m) return fail_with(FDDM_ERR_INVALID, "fewer data points than varying parameters");
+  if (nx == 0 || ny == 0) return fail_with(FDDM_ERR_INVALID, "no abscissa or data rows");
   if (m > (1ull << 30) || nproblems > (1ull << 30) || nchains > (1ull << 30) || ny > (1ull << 30) ||
-      nw > (1ull << 30))
+      nw > (1ull << 30) || nx > (1ull << 30))
     return fail_with(FDDM_ERR_UNSUPPORTED, "too many data points, problems or chains");
   if (!options) return fail_with(FDDM_ERR_INVALID, "null options");
   if (nchains == 0 || nproblems == 0) return FDDM_OK;
   if (!d_x || !d_y || !d_problems || !d_chain_offsets || !d_chain_problems || !d_init || !d_min || !d_max ||
       !d_values || !d_stderr || !d_chisqr || !d_nfev || !d_info || !d_status || !d_workspace)
     return fail_with(FDDM_ERR_INVALID, "null pointer argument");
-  if (ldy < m || (d_w && ldw < m)) return fail_with(FDDM_ERR_INVALID, "row stride shorter than the data");
+  if (ldx < m || ldy < m || (d_w && ldw < m)) return fail_with(FDDM_ERR_INVALID, "row stride shorter than the data");
   const uint64_t per_slot = (uint64_t)slot_doubles(m, np) * sizeof(double);
   const int group = group_warps(nchains);
   const uint64_t slots = std::min<uint64_t>({nchains, max_slots(group), workspace_bytes / per_slot});
@@ -74,6 +76,8 @@ extern "C" int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, const 
   b.np = np;
   b.m = (int)m;
   b.x = d_x;
+  b.ldx = ldx;
+  b.nx = (int)nx;
   b.y = d_y;
   b.ldy = ldy;
   b.ny = (int)ny;

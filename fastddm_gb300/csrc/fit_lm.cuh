@@ -20,7 +20,7 @@
 // Layout.  A group of threads runs one chain of fits (a fit_multik sweep
 // warm-starts each fit from the previous result, so a chain is sequential):
 // one warp when there are many chains, or the W = 4 warps of a CTA when there
-// are at most as many chains as SMs, so that the per-point work of a chain is
+// are at most two chains per SM, so that the per-point work of a chain is
 // spread over the four sub-partitions of its SM (on GB300 an FP64 instruction
 // occupies a sub-partition's FP64 pipe for about 64 cycles whatever the
 // number of active lanes, and a single chain is bound by that latency).  The
@@ -242,8 +242,10 @@ __device__ __forceinline__ double norm_n(const double (&v)[N]) {
 }
 
 struct Batch {
-  int model, np, m;
-  const double* x;
+  int model, np, m;  // m: the largest number of points of a problem (workspace and residual rows)
+  const double* x;   // abscissae rows, row r at x + r * ldx
+  uint64_t ldx;
+  int nx;            // rows of x
   const double* y;
   uint64_t ldy;
   int ny;  // rows of y
@@ -251,7 +253,7 @@ struct Batch {
   uint64_t ldw;
   int nw;  // rows of w
   int nprob;
-  const int32_t* problems;  // [nprob][4]: y row, w row (-1: none), pred (-1: none), vary mask
+  const int32_t* problems;  // [nprob][6]: y row, w row (-1: none), pred (-1: none), vary mask, x row, points
   const int32_t* chain_off;
   const int32_t* chain_list;
   int nchains;
@@ -277,8 +279,10 @@ template <int NV, int W>
 struct Fit {
   const Batch& b;
   Grp<W>& G;
+  const double* x;  // this problem's abscissae, m of them
   const double* y;
   const double* w;
+  int m;
   double* fj[NV];
   double pe[kMaxP];  // external values (fixed ones are constant)
   int vix[NV];       // parameter index of each varying parameter
@@ -314,8 +318,8 @@ struct Fit {
   __device__ double evaluate(double* out, const double* fv, double rfd) {
     double s = 0.0;
     bool bad = false;
-    for (int i = G.tid; i < b.m; i += 32 * W) {
-      double r = model_eval(b.model, b.x[i], pe) - y[i];
+    for (int i = G.tid; i < m; i += 32 * W) {
+      double r = model_eval(b.model, x[i], pe) - y[i];
       if (w) r = r * w[i];
       bad |= !isfinite(r);
       if (rfd != 0.0) r = (r - fv[i]) * rfd;
@@ -338,7 +342,7 @@ struct Fit {
 template <int NV, int W>
 __device__ void qr_pivot(Fit<NV, W>& F, const double (&colsq)[NV], double* wt, double (&R)[NV][NV], int (&ipvt)[NV],
                          double (&acnorm)[NV], double (&qtf)[NV]) {
-  const int m = F.b.m, tid = F.G.tid;
+  const int m = F.m, tid = F.G.tid;
   constexpr int S = 32 * W;
   double rdiag[NV], wa[NV];
   bool recomp[NV];
@@ -653,7 +657,7 @@ __device__ void lmdif(Fit<NV, W>& F, double (&u)[NV], double*& fv, double*& wt, 
       F.set_one(j, keep);
       if (F.status != kOk) return;
     }
-    for (int i = F.G.tid; i < b.m; i += 32 * W) wt[i] = fv[i];
+    for (int i = F.G.tid; i < F.m; i += 32 * W) wt[i] = fv[i];
     qr_pivot(F, colsq, wt, R, ipvt, acnorm, qtf);
     if (iter == 1) {
 #pragma unroll
@@ -758,13 +762,14 @@ __device__ void lmdif(Fit<NV, W>& F, double (&u)[NV], double*& fv, double*& wt, 
 template <int NV, int W>
 __device__ void run_problem(const Batch& b, int prob, double* slot, Grp<W>& G) {
   const int lane = G.tid;
-  const int32_t* pr = b.problems + 4 * (size_t)prob;
+  const int32_t* pr = b.problems + 6 * (size_t)prob;
   const int yrow = pr[0], wrow = pr[1], pred = pr[2];
   const uint32_t vary = (uint32_t)pr[3];
+  const int xrow = pr[4], mp = pr[5];
   // a problem naming a row or a predecessor that does not exist, or varying another number of
   // parameters than the launch, is not fitted
-  if (yrow < 0 || yrow >= b.ny || wrow >= b.nw || (wrow >= 0 && !b.w) || pred >= b.nprob ||
-      __popc(vary & ((1u << b.np) - 1u)) != NV || (vary >> b.np) != 0u) {
+  if (yrow < 0 || yrow >= b.ny || wrow >= b.nw || (wrow >= 0 && !b.w) || pred >= b.nprob || xrow < 0 ||
+      xrow >= b.nx || mp < NV || mp > b.m || __popc(vary & ((1u << b.np) - 1u)) != NV || (vary >> b.np) != 0u) {
     if (lane == 0) {
       for (int p = 0; p < b.np; ++p) {
         b.values[(size_t)prob * b.np + p] = NAN;
@@ -779,6 +784,8 @@ __device__ void run_problem(const Batch& b, int prob, double* slot, Grp<W>& G) {
     return;
   }
   Fit<NV, W> F(b, G);
+  F.m = mp;
+  F.x = b.x + (size_t)xrow * b.ldx;
   F.y = b.y + (size_t)yrow * b.ldy;
   F.w = wrow >= 0 ? b.w + (size_t)wrow * b.ldw : nullptr;
   double* fv = slot;
@@ -856,7 +863,7 @@ __device__ void run_problem(const Batch& b, int prob, double* slot, Grp<W>& G) {
           Ui[i][c] = i <= c ? s * rd[i] : 0.0;
         }
       }
-      const int nfree = b.m - NV;
+      const int nfree = mp - NV;
       const double redchi = fsq / (double)(nfree > 1 ? nfree : 1);
       // variance of the parameter at position i: row i of Ui squared
 #pragma unroll
@@ -890,7 +897,7 @@ __device__ void run_problem(const Batch& b, int prob, double* slot, Grp<W>& G) {
     b.status[prob] = F.status;
   }
   if (b.residual)
-    for (int i = G.tid; i < b.m; i += 32 * W) b.residual[(size_t)prob * b.m + i] = fv[i];
+    for (int i = G.tid; i < mp; i += 32 * W) b.residual[(size_t)prob * b.m + i] = fv[i];
   G.sync();
 }
 

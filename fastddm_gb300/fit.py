@@ -150,23 +150,13 @@ def _copy(d):
     return copy.deepcopy(d) if d is not None else None
 
 
-def fit_multik(data: Union[AzimuthalAverage, IntermediateScatteringFunction], model: Model, ref: int,
-               ref_params: Optional[Parameters] = None, return_model_results: Optional[bool] = False,
-               use_err: Optional[bool] = False, fixed_params: Optional[Dict[str, Sequence[float]]] = None,
-               fixed_params_min: Optional[Dict[str, Sequence[float]]] = None,
-               fixed_params_max: Optional[Dict[str, Sequence[float]]] = None,
-               fixed_params_expr: Optional[Dict[str, Sequence[str]]] = None, *, warm_start: str = "chain",
-               gpu_id: int = 0, **fitargs: Any) -> Tuple[FitTable, Optional[List[Optional[ModelResult]]]]:
-    """Fit ``model`` to every k of ``data`` on the GPU (fit.py:197-397).
+class _Sweep:
+    """The device problems of one fit_multik call (rows, warm starts, launches) and what
+    turns their results into the reference's table."""
 
-    Parameters as the reference: the fit at ``ref`` starts from the model's
-    values (updated by ``ref_params`` and parameter values given as keyword
-    arguments); the sweeps ref-1 .. 0 and ref .. K-1 start each fit from the
-    previous one; ``use_err`` weights each k by 1 / ``data.err[k]``;
-    ``fixed_params*`` give per-k values and bounds.  Rows whose first value is
-    NaN are skipped (NaN results).  ``warm_start``: "chain" (the reference's
-    sweep), "ref" or "none" (see the module docstring).
-    """
+
+def _sweep(data, model: Model, ref: int, ref_params, use_err, fixed_params, fixed_params_min, fixed_params_max,
+           fixed_params_expr, warm_start: str, fitargs: Dict[str, Any]) -> _Sweep:
     if fixed_params_expr:
         raise NotImplementedError("fixed_params_expr: parameter expressions are not supported by the device fits")
     if warm_start not in ("chain", "ref", "none"):
@@ -270,11 +260,24 @@ def fit_multik(data: Union[AzimuthalAverage, IntermediateScatteringFunction], mo
     bad = ~np.all(np.isfinite(Y[ks]), axis=1)
     if np.any(bad):  # lmfit refuses data with NaN (nan_policy 'raise') at the first such fit
         raise ValueError("The input contains nan values")
-    problems = np.stack([ks, wr, pred, np.full(ks.size, base.vary)], axis=1).astype(np.int32)
-    out = run_fits(model, tau, Y, W, problems, stages, init[ks], lo[ks], hi[ks], options, gpu_id)
-    if np.any(out["status"] == ST_NONFINITE):
-        raise ValueError(NAN_MESSAGE)
+    problems = np.stack([ks, wr, pred, np.full(ks.size, base.vary), np.zeros(ks.size, np.int64),
+                         np.full(ks.size, tau.size)], axis=1).astype(np.int32)
+    sw = _Sweep()
+    sw.model, sw.names, sw.K, sw.tau, sw.Y, sw.W = model, names, K, tau, Y, W
+    sw.problems, sw.stages, sw.init, sw.lo, sw.hi = problems, stages, init[ks], lo[ks], hi[ks]
+    sw.ks, sw.wr, sw.pred, sw.base, sw.model_params = ks, wr, pred, base, model_params
+    sw.k = np.asarray(data.k)
+    sw.options, sw.scale_covar, sw.calc_covar = options, scale_covar, calc_covar
+    sw.init_k, sw.lo_k, sw.hi_k = init, lo, hi
+    return sw
 
+
+def _sweep_results(sw: _Sweep, out: Dict[str, Any], return_model_results: bool):
+    """The reference's table (and ModelResults) from the library's outputs for this sweep's problems."""
+    model, names, K, tau, Y, W = sw.model, sw.names, sw.K, sw.tau, sw.Y, sw.W
+    ks, wr, pred, base, model_params = sw.ks, sw.wr, sw.pred, sw.base, sw.model_params
+    init, lo, hi = sw.init_k, sw.lo_k, sw.hi_k
+    scale_covar, calc_covar = sw.scale_covar, sw.calc_covar
     # each k's result is its last fit (the refit at ref replaces the first fit there)
     final = np.full(K, -1)
     final[ks] = np.arange(ks.size)
@@ -300,7 +303,7 @@ def fit_multik(data: Union[AzimuthalAverage, IntermediateScatteringFunction], mo
     ok = (out["info"] >= 1) & (out["info"] <= 4) & (out["status"] == 0)
     results["success"] = np.zeros(K, dtype=bool)
     results["success"][have] = ok[final[have]]
-    results["k"] = np.asarray(data.k)
+    results["k"] = sw.k
     model_results: Optional[List[Optional[ModelResult]]] = None
     if return_model_results:
         model_results = [None] * K
@@ -316,3 +319,107 @@ def fit_multik(data: Union[AzimuthalAverage, IntermediateScatteringFunction], mo
             w = None if wr[pi] < 0 else W[wr[pi]]
             model_results[k] = ModelResult(model, start, Y[k], tau, w, out, pi, scale_covar, calc_covar)
     return FitTable(results, out["device_ms"], out["launches"]), model_results
+
+
+def fit_multik(data: Union[AzimuthalAverage, IntermediateScatteringFunction], model: Model, ref: int,
+               ref_params: Optional[Parameters] = None, return_model_results: Optional[bool] = False,
+               use_err: Optional[bool] = False, fixed_params: Optional[Dict[str, Sequence[float]]] = None,
+               fixed_params_min: Optional[Dict[str, Sequence[float]]] = None,
+               fixed_params_max: Optional[Dict[str, Sequence[float]]] = None,
+               fixed_params_expr: Optional[Dict[str, Sequence[str]]] = None, *, warm_start: str = "chain",
+               gpu_id: int = 0, **fitargs: Any) -> Tuple[FitTable, Optional[List[Optional[ModelResult]]]]:
+    """Fit ``model`` to every k of ``data`` on the GPU (fit.py:197-397).
+
+    Parameters as the reference: the fit at ``ref`` starts from the model's
+    values (updated by ``ref_params`` and parameter values given as keyword
+    arguments); the sweeps ref-1 .. 0 and ref .. K-1 start each fit from the
+    previous one; ``use_err`` weights each k by 1 / ``data.err[k]``;
+    ``fixed_params*`` give per-k values and bounds.  Rows whose first value is
+    NaN are skipped (NaN results).  ``warm_start``: "chain" (the reference's
+    sweep), "ref" or "none" (see the module docstring).
+    """
+    sw = _sweep(data, model, ref, ref_params, use_err, fixed_params, fixed_params_min, fixed_params_max,
+                fixed_params_expr, warm_start, dict(fitargs))
+    out = run_fits(sw.model, sw.tau[None, :], sw.Y, sw.W, sw.problems, sw.stages, sw.init, sw.lo, sw.hi,
+                   sw.options, gpu_id)
+    if np.any(out["status"] == ST_NONFINITE):
+        raise ValueError(NAN_MESSAGE)
+    return _sweep_results(sw, out, bool(return_model_results))
+
+
+def fit_multik_batch(jobs: Sequence[Dict[str, Any]], model: Model, *, warm_start: str = "chain", gpu_id: int = 0,
+                     return_model_results: bool = False, **common: Any
+                     ) -> List[Tuple[FitTable, Optional[List[Optional[ModelResult]]]]]:
+    """``fit_multik`` of many datasets in one pair of device launches.
+
+    Each job is a dict with ``data`` and ``ref`` and any other argument of
+    :func:`fit_multik` for that dataset (``ref_params``, ``use_err``,
+    ``fixed_params``..., parameter values such as ``A=``); ``common`` holds
+    arguments shared by every job (``fit_kws``, ``max_nfev``, ``weights``...).
+    Datasets may differ in their number of k and of lags.  Every fit gives
+    what it gives in a ``fit_multik`` call of its own; all sweeps run
+    concurrently, the fits at the jobs' ``ref`` first.  The jobs must vary the
+    same number of parameters.  Returns one (table, model results) per job.
+    """
+    if not jobs:
+        return []
+    sweeps = []
+    for job in jobs:
+        kw = dict(common)
+        kw.update({k: v for k, v in job.items() if k not in ("data", "ref")})
+        args = [kw.pop(n, None) for n in ("ref_params", "use_err", "fixed_params", "fixed_params_min",
+                                           "fixed_params_max", "fixed_params_expr")]
+        args[1] = bool(args[1])
+        sweeps.append(_sweep(job["data"], model, job["ref"], *args, warm_start, kw))
+    options = sweeps[0].options
+    if any(not np.array_equal(sw.options, options) for sw in sweeps):
+        raise ValueError("the jobs of one batch share fit_kws and max_nfev")
+    nv = {int(sw.base.vary) for sw in sweeps}
+    if len({bin(v).count("1") for v in nv}) != 1:
+        raise ValueError("the jobs of one batch must vary the same number of parameters")
+    m = max(sw.tau.size for sw in sweeps)
+
+    def pad(a):
+        out = np.zeros((a.shape[0], m))
+        out[:, : a.shape[1]] = a
+        return out
+
+    X = np.stack([np.pad(sw.tau, (0, m - sw.tau.size)) for sw in sweeps])
+    Ys, Ws, probs, inits, los, his = [], [], [], [], [], []
+    nstage = max(len(sw.stages) for sw in sweeps)
+    stages: List[List[List[int]]] = [[] for _ in range(nstage)]
+    yoff = woff = poff = 0
+    offsets = []
+    for i, sw in enumerate(sweeps):
+        pr = sw.problems.astype(np.int64).copy()
+        pr[:, 0] += yoff
+        pr[:, 1] = np.where(pr[:, 1] >= 0, pr[:, 1] + woff, -1)
+        pr[:, 2] = np.where(pr[:, 2] >= 0, pr[:, 2] + poff, -1)
+        pr[:, 4] = i
+        probs.append(pr)
+        Ys.append(pad(sw.Y))
+        if sw.W is not None:
+            Ws.append(pad(sw.W))
+        inits.append(sw.init)
+        los.append(sw.lo)
+        his.append(sw.hi)
+        # a sweep with one launch (warm_start "none") runs with the others' second launch
+        first = nstage - len(sw.stages)
+        for s, chains in enumerate(sw.stages):
+            stages[first + s].extend([[p + poff for p in c] for c in chains])
+        offsets.append(poff)
+        yoff += sw.Y.shape[0]
+        woff += 0 if sw.W is None else sw.W.shape[0]
+        poff += pr.shape[0]
+    W = np.concatenate(Ws) if Ws else None
+    out = run_fits(sweeps[0].model, X, np.concatenate(Ys), W, np.concatenate(probs).astype(np.int32),
+                   [st for st in stages if st], np.concatenate(inits), np.concatenate(los), np.concatenate(his),
+                   options, gpu_id)
+    results = []
+    for i, (sw, off) in enumerate(zip(sweeps, offsets)):
+        n = sw.problems.shape[0]
+        part = {k: (v[off:off + n] if isinstance(v, np.ndarray) else v) for k, v in out.items()}
+        if np.any(part["status"] == ST_NONFINITE):
+            raise ValueError(f"job {i}: " + NAN_MESSAGE)
+        results.append(_sweep_results(sw, part, return_model_results))
+    return results

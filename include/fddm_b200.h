@@ -342,18 +342,19 @@ int fddm_b200_experiment_dft_stage(int variant, const void* d_rows, uint64_t npa
      FDDM_FIT_FLORY_SCHULZ_SF   A, B, Gamma, sigma    :971
      FDDM_FIT_SIMPLE_EXP        tau, amplitude        fit.py:67
      FDDM_FIT_SIMPLE_SF         A, B, tau             fit.py:84
-   A problem is one curve: y row d_y + row*ldy of ny rows (m points at
-   abscissae d_x), weights row d_w + wrow*ldw of nw rows or none (residual
-   (model - y) * w), starting
-   values, bounds (+-INFINITY for none) and the mask of varying parameters.
-   d_problems holds 4 int32 per problem: y row, weight row (-1: none), pred
-   (-1: none), vary mask (bit p: parameter p varies; the same number nvary of
-   set bits in every problem).  With pred >= 0 the varying parameters start
+   A problem is one curve of mp <= m points: abscissae row d_x + xrow*ldx (nx
+   rows), data row d_y + row*ldy (ny rows), weights row d_w + wrow*ldw (nw
+   rows) or none (residual (model - y) * w), starting values, bounds
+   (+-INFINITY for none) and the mask of varying parameters.  d_problems holds
+   6 int32 per problem: y row, weight row (-1: none), pred (-1: none), vary
+   mask (bit p: parameter p varies; the same number nvary of set bits in every
+   problem), x row, mp (nvary <= mp <= m).  With pred >= 0 the varying parameters start
    from problem pred's fitted values instead of d_init (fit_multik's warm
    start); pred must come earlier in the same chain or have been fitted by an
    earlier call.  Starting values are clipped into [min, max] as lmfit does.
    Chains: chain c runs problems d_chain_problems[d_chain_offsets[c] ..
-   d_chain_offsets[c+1]-1] in order on one warp; chains run concurrently.
+   d_chain_offsets[c+1]-1] in order on one warp, or on a CTA of four warps
+   when there are at most two chains per SM; chains run concurrently.
    d_init, d_min, d_max, d_values, d_stderr: [nproblems][nparams] doubles.
    options (host, 6 doubles): ftol, xtol, gtol, epsfcn, factor, max_nfev
    (<= 0: 2000*(nvary+1)); lmfit's defaults are 1e-7, 1e-7, 1e-7, 0, 100, 0.
@@ -364,10 +365,12 @@ int fddm_b200_experiment_dft_stage(int variant, const void* d_rows, uint64_t npa
    finish), chi^2, function evaluations, MINPACK's info (1-4
    converged, 6-8 tolerance too small, -1 aborted), status (0 done, 1 a
    residual was not finite: the reference raises ValueError there and the
-   chain stops, 2 aborted after max_nfev evaluations, 3 not fitted: a row or
-   predecessor out of range or another number of varying parameters; a
+   chain stops, 2 aborted after max_nfev evaluations, 3 not fitted: a row,
+   predecessor or point count out of range or another number of varying
+   parameters; a
    chain also ends at an entry that is not a problem), and optionally the
-   final residuals ([nproblems][m], d_residual may be NULL).
+   final residuals ([nproblems][m], the first mp of each row; d_residual may
+   be NULL).
    The workspace holds (2 + nparams) * m doubles per concurrently running
    chain; fddm_b200_fit_workspace_bytes gives the size that runs every chain
    at once (a smaller one runs fewer at a time, down to one). */
@@ -381,8 +384,9 @@ int fddm_b200_experiment_dft_stage(int variant, const void* d_rows, uint64_t npa
 #define FDDM_FIT_SIMPLE_SF 7
 int fddm_b200_fit_model_nparams(int model);
 int fddm_b200_fit_workspace_bytes(int model, uint64_t m, uint64_t nchains, uint64_t* bytes);
-int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, const double* d_y, uint64_t ldy, uint64_t ny,
-                     const double* d_w, uint64_t ldw, uint64_t nw, const int32_t* d_problems, uint64_t nproblems,
+int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, uint64_t ldx, uint64_t nx, const double* d_y,
+                     uint64_t ldy, uint64_t ny, const double* d_w, uint64_t ldw, uint64_t nw,
+                     const int32_t* d_problems, uint64_t nproblems,
                      const int32_t* d_chain_offsets,
                      const int32_t* d_chain_problems, uint64_t nchains, int nvary, const double* d_init,
                      const double* d_min, const double* d_max, const double* options, double* d_values,

@@ -152,7 +152,7 @@ class FakeDevice:
             self.launches.append([list(c) for c in chains])
             for chain in chains:
                 for pi in chain:
-                    row, wrow, pred, vary = (int(v) for v in problems[pi])
+                    row, wrow, pred, vary, xrow, npts = (int(v) for v in problems[pi])
                     assert pred < 0 or pred in done  # a warm start only reads a finished fit
                     par = {}
                     for i, n in enumerate(self.names):
@@ -160,7 +160,8 @@ class FakeDevice:
                         if (vary >> i) & 1 and pred >= 0:
                             v = vals[pred][i]
                         par[n] = {"value": v, "min": lo[pi][i], "max": hi[pi][i], "vary": bool((vary >> i) & 1)}
-                    r = fo.lm_fit(self.func, self.names, par, x, Y[row], None if wrow < 0 else W[wrow])
+                    r = fo.lm_fit(self.func, self.names, par, x[xrow, :npts], Y[row, :npts],
+                                  None if wrow < 0 else W[wrow, :npts])
                     vals[pi] = [r["values"][n] for n in self.names]
                     se[pi] = [-1.0 if r["stderr"][n] is None else r["stderr"][n] for n in self.names]
                     out["chisqr"][pi] = r["chisqr"]
@@ -285,3 +286,23 @@ def test_lmfit_models_and_parameters_are_converted(monkeypatch):
     ref_params = {"A": LmParam("A", A[3], min=EPS), "B": LmParam("B", B[3]), "Gamma": LmParam("Gamma", G[3], min=EPS)}
     table, _ = gfit.fit_multik(aa, m, 3, ref_params=ref_params)
     np.testing.assert_allclose(table["Gamma"], G, rtol=0.05)
+
+
+def test_fit_multik_batch_gives_each_job_its_own_result(monkeypatch):
+    """Datasets of different sizes (k and lags) in one batch: each table equals its own fit_multik."""
+    a1, (A1, B1, G1) = synthetic_aa(K=10, m=40, seed=5, nan_rows=(2,))
+    a2, (A2, B2, G2) = synthetic_aa(K=14, m=60, seed=6)
+    m = fit_models.simple_exponential_model
+    fake = FakeDevice("simple_exponential_model")
+    monkeypatch.setattr(gfit, "run_fits", fake)
+    jobs = [dict(data=a1, ref=4, A=A1[4], B=B1[4], Gamma=G1[4], use_err=True),
+            dict(data=a2, ref=9, A=A2[9], B=B2[9], Gamma=G2[9], fixed_params_min={"B": np.zeros(14)})]
+    batch = gfit.fit_multik_batch(jobs, m)
+    assert len(fake.launches) == 2 and len(fake.launches[0]) == 2 and len(fake.launches[1]) == 4
+    alone = [gfit.fit_multik(a1, m, 4, A=A1[4], B=B1[4], Gamma=G1[4], use_err=True)[0],
+             gfit.fit_multik(a2, m, 9, A=A2[9], B=B2[9], Gamma=G2[9], fixed_params_min={"B": np.zeros(14)})[0]]
+    for (tb, _), ta in zip(batch, alone):
+        for col in ta.columns:
+            np.testing.assert_array_equal(tb[col], ta[col], err_msg=col)
+    with pytest.raises(ValueError, match="same number"):
+        gfit.fit_multik_batch([dict(data=a1, ref=4), dict(data=a2, ref=9, fixed_params={"B": B2})], m)

@@ -248,3 +248,31 @@ def test_evaluation_limit_stops_the_fit():
     m = fit_models.generic_exponential_model
     r = m.fit(y, params=m.make_params(**CASES["generic_exponential_model"][1]), x=x, max_nfev=12)
     assert not r.success and r.aborted and r.nfev == 13
+
+
+def test_fit_multik_batch_matches_single_calls():
+    """Three datasets of different sizes in one batch (six sweeps, a CTA each, as in single calls):
+    bit-identical to fit_multik on each; 200 datasets (400 sweeps, a warp each): within tolerance."""
+    from fastddm_gb300 import fit as gfit
+    from fastddm_gb300 import fit_models
+
+    m = fit_models.simple_exponential_model
+    sets = [_aa(K=K, m=mm, seed=s) for K, mm, s in ((30, 80, 1), (48, 120, 2), (20, 60, 3))]
+    jobs = [dict(data=a, ref=len(a.k) // 3, A=A[len(a.k) // 3], B=B[len(a.k) // 3], Gamma=G[len(a.k) // 3],
+                 use_err=True) for a, (A, B, G) in sets]
+    batch = gfit.fit_multik_batch(jobs, m)
+    for job, (tb, _) in zip(jobs, batch):
+        kw = {k: v for k, v in job.items() if k not in ("data", "ref")}
+        ta, _ = gfit.fit_multik(job["data"], m, job["ref"], **kw)
+        for col in ta.columns:
+            np.testing.assert_array_equal(tb[col], ta[col], err_msg=col)
+    many = [_aa(K=24, m=50 + (s % 7) * 10, seed=100 + s) for s in range(200)]
+    jobs = [dict(data=a, ref=8, A=A[8], B=B[8], Gamma=G[8], use_err=True) for a, (A, B, G) in many]
+    batch = gfit.fit_multik_batch(jobs, m)
+    for job, (tb, _) in zip(jobs[:10], batch[:10]):
+        kw = {k: v for k, v in job.items() if k not in ("data", "ref")}
+        ta, _ = gfit.fit_multik(job["data"], m, job["ref"], **kw)
+        np.testing.assert_array_equal(tb["success"], ta["success"])
+        for p in ("A", "Gamma"):
+            tol = np.maximum(PAR_TOL * np.abs(ta[p]), SE_FRAC * ta[f"{p}_stderr"])
+            assert np.all(np.abs(tb[p] - ta[p]) <= tol), p
