@@ -978,12 +978,16 @@ def serve_records(args, n_req: int, device) -> dict:
     total_frames = sum(sc.length for sc in scenes)
     checked = list(range(0, n_req, max(1, n_req // 8)))[:8]
 
-    def requests():
-        return [Request(i, frames[i], np.arange(1, scenes[i].length), "fft", None, float(arrivals[i]))
+    def requests(scale):
+        return [Request(i, frames[i], np.arange(1, scenes[i].length), "fft", None, float(arrivals[i] * scale))
                 for i in range(n_req)]
 
     results = {}
-    for label, prec, streams in (("continuous_batching", args.precision, 6), ("one_at_a_time_f64", "f64", 1)):
+    # the stream as specified; the same stream arriving 10x faster (a queue forms, so small requests
+    # admitted together share a batched launch); one request at a time in FP64
+    for label, prec, streams, scale in (("continuous_batching", args.precision, 6, 1.0),
+                                        ("continuous_batching_10x_rate", args.precision, 6, 0.1),
+                                        ("one_at_a_time_f64", "f64", 1, 1.0)):
         torch.cuda.empty_cache()
         free, _ = torch.cuda.mem_get_info(device)
         ex = GpuExecutor(0, prec, streams, pool_bytes=int(0.35 * free))
@@ -1004,16 +1008,17 @@ def serve_records(args, n_req: int, device) -> dict:
 
         def deliver(r):  # the client takes each result; a few are kept for the identity check
             res = server.fetch(r.rid)
-            if r.rid in checked and label == "continuous_batching":
+            if r.rid in checked and label.startswith("continuous_batching"):
                 kept[r.rid] = res
 
-        reqs = replay(server, requests(), time.perf_counter, deliver=deliver)
+        reqs = replay(server, requests(scale), time.perf_counter, deliver=deliver)
         span = max(r.completed for r in reqs) - min(r.arrival for r in reqs)
         summ = latency_summary(reqs)
         summ.update({"frames_per_s": total_frames / span, "span_s": span, "peak_inflight": server.peak_inflight,
-                     "batched_launches": server.batches, "slots": streams, "precision": prec})
+                     "batched_launches": server.batches, "slots": streams, "precision": prec,
+                     "arrival_rate_per_s": 50.0 / scale})
         results[label] = summ
-        if label == "continuous_batching":
+        if label.startswith("continuous_batching"):
             # a few results again, each alone on an idle device: must be identical
             same = True
             for i in checked:
