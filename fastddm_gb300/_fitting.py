@@ -197,7 +197,8 @@ def check_bounds(lo: np.ndarray, hi: np.ndarray, names: Sequence[str]):
 
 def run_fits(model: "Model", X: np.ndarray, Y: np.ndarray, W: Optional[np.ndarray], problems: np.ndarray,
              stages: Sequence[Sequence[Sequence[int]]], init: np.ndarray, lo: np.ndarray, hi: np.ndarray,
-             options: np.ndarray, gpu_id: int = 0, residual: bool = False) -> Dict[str, np.ndarray]:
+             options: np.ndarray, gpu_id: int = 0, residual: bool = False,
+             covariance: bool = False) -> Dict[str, np.ndarray]:
     """Run the fits on the device.
 
     X, Y, W: rows of abscissae, data and weights (W may be None), as wide as
@@ -236,6 +237,7 @@ def run_fits(model: "Model", X: np.ndarray, Y: np.ndarray, W: Optional[np.ndarra
     info = torch.empty(P, **i32)
     status = torch.empty(P, **i32)
     res = torch.empty((P, m), **f64) if residual else None
+    cov = torch.empty((P, npar, npar), **f64) if covariance else None
     most = max(len(s) for s in stages)
     nbytes = ctypes.c_uint64(0)
     _lib.check(lib.fddm_b200_fit_workspace_bytes(model.device_id, m, most, ctypes.byref(nbytes)))
@@ -259,7 +261,8 @@ def run_fits(model: "Model", X: np.ndarray, Y: np.ndarray, W: Optional[np.ndarra
                 dprob.data_ptr(), P, doff.data_ptr(), dlist.data_ptr(), nch, nvary,
                 dinit.data_ptr(), dlo.data_ptr(), dhi.data_ptr(), opts.ctypes.data,
                 vals.data_ptr(), se.data_ptr(), chisqr.data_ptr(), nfev.data_ptr(), info.data_ptr(),
-                status.data_ptr(), None if res is None else res.data_ptr(), ws.data_ptr(), ws.numel() * 8,
+                status.data_ptr(), None if res is None else res.data_ptr(), None if cov is None else cov.data_ptr(),
+                ws.data_ptr(), ws.numel() * 8,
                 stream.cuda_stream))
         t1.record(stream)
         stream.synchronize()
@@ -268,6 +271,8 @@ def run_fits(model: "Model", X: np.ndarray, Y: np.ndarray, W: Optional[np.ndarra
            "nvary": nvary, "device_ms": t0.elapsed_time(t1), "launches": len(chain_tabs)}
     if res is not None:
         out["residual"] = res.cpu().numpy()
+    if cov is not None:
+        out["covar"] = cov.cpu().numpy()
     if np.any(out["status"] == ST_INVALID):
         raise RuntimeError("fit problems named rows or predecessors that do not exist")
     return out
@@ -320,7 +325,19 @@ class ModelResult:
             else:
                 p.stderr = s / math.sqrt(self.redchi) if self.redchi > 0 else s
         self.best_values = {n: self.params[n].value for n in names}
-        self.covar = None  # the library returns the standard errors, not the covariance
+        # lmfit's covar: the varying parameters' covariance in var_names order (None without one)
+        self.covar = None
+        if "covar" in out and calc_covar:
+            idx = [i for i, n in enumerate(names) if params[n].vary]
+            c = out["covar"][k][np.ix_(idx, idx)]
+            if np.all(np.isfinite(c)) and all(self.params[n].stderr is not None for n in self.var_names):
+                if not scale_covar and self.redchi > 0:
+                    c = c / self.redchi
+                self.covar = c
+                for a, na in enumerate(self.var_names):
+                    pa = self.params[na]
+                    pa.correl = {nb: float(c[a, b] / np.sqrt(c[a, a] * c[b, b]))
+                                 for b, nb in enumerate(self.var_names) if b != a}
         self.residual = out["residual"][k] if "residual" in out else None
 
     @property
@@ -456,7 +473,7 @@ class Model:
         spec = FitSpec(self, params)
         problems = np.array([[0, 0 if W is not None else -1, -1, spec.vary, 0, y.size]], dtype=np.int32)
         out = run_fits(self, x[None, :], y[None, :], W, problems, [[[0]]], spec.init[None], spec.lo[None], spec.hi[None],
-                       lsq_options(fit_kws, max_nfev), gpu_id, residual=True)
+                       lsq_options(fit_kws, max_nfev), gpu_id, residual=True, covariance=calc_covar)
         if int(out["status"][0]) == ST_NONFINITE:
             raise ValueError(NAN_MESSAGE)
         r = ModelResult(self, params, y, x, None if W is None else W[0], out, 0, scale_covar, calc_covar)

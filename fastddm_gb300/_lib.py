@@ -130,7 +130,7 @@ _SIGNATURES = {
     "fddm_b200_fit_lm": (
         ctypes.c_int,
         [ctypes.c_int, _u64, _vp, _u64, _u64, _vp, _u64, _u64, _vp, _u64, _u64, _vp, _u64, _vp, _vp, _u64,
-         ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u64, _vp],
+         ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u64, _vp],
     ),
     "fddm_b200_tiff_info": (
         ctypes.c_int,

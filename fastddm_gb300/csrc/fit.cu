@@ -51,7 +51,7 @@ extern "C" int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, uint64
                                 int nvary, const double* d_init, const double* d_min, const double* d_max,
                                 const double* options, double* d_values, double* d_stderr, double* d_chisqr,
                                 int32_t* d_nfev, int32_t* d_info, int32_t* d_status, double* d_residual,
-                                void* d_workspace, uint64_t workspace_bytes, void* stream) {
+                                double* d_covar, void* d_workspace, uint64_t workspace_bytes, void* stream) {
   set_last_error("");
   const int np = fitlm::model_nparams(model);
   if (np == 0) return fail_with(FDDM_ERR_INVALID, "unknown fit model");
@@ -105,6 +105,7 @@ extern "C" int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, uint64
   b.info = d_info;
   b.status = d_status;
   b.residual = d_residual;
+  b.covar = d_covar;
   b.ws = static_cast<double*>(d_workspace);
   b.slot_doubles = slot_doubles(m, np);
   b.nslots = (int)slots;

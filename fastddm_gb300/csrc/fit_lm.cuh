@@ -269,6 +269,7 @@ struct Batch {
   int32_t* info;
   int32_t* status;
   double* residual;  // [nprob][m] or null
+  double* covar;     // [nprob][np][np] or null
   double* ws;
   size_t slot_doubles;
   int nslots;
@@ -873,10 +874,30 @@ __device__ void run_problem(const Batch& b, int prob, double* slot, Grp<W>& G) {
         for (int k = 0; k < NV; ++k) s += Ui[i][k] * Ui[i][k];
         put(se, ipvt[i], sqrt(s * redchi));
       }
+      // the whole covariance, when asked for: entry (p, q) of the parameters at positions i, k
+      if (b.covar && lane == 0) {
+        double* co = b.covar + (size_t)prob * b.np * b.np;
+        for (int e = 0; e < b.np * b.np; ++e) co[e] = 0.0;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+          const int pi = sel(F.vix, ipvt[i]);
+#pragma unroll
+          for (int k = 0; k < NV; ++k) {
+            double s = 0.0;
+#pragma unroll
+            for (int l = 0; l < NV; ++l) s += Ui[i][l] * Ui[k][l];
+            co[pi * b.np + sel(F.vix, ipvt[k])] = s * redchi;
+          }
+        }
+      }
     } else if (cov == 1) {
 #pragma unroll
       for (int k = 0; k < NV; ++k) se[k] = NAN;
     }
+  }
+  if (b.covar && lane == 0 && cov != 0) {  // no finite covariance: NaN
+    double* co = b.covar + (size_t)prob * b.np * b.np;
+    for (int e = 0; e < b.np * b.np; ++e) co[e] = NAN;
   }
   if (lane == 0) {
     double* vo = b.values + (size_t)prob * b.np;

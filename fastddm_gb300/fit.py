@@ -341,7 +341,7 @@ def fit_multik(data: Union[AzimuthalAverage, IntermediateScatteringFunction], mo
     sw = _sweep(data, model, ref, ref_params, use_err, fixed_params, fixed_params_min, fixed_params_max,
                 fixed_params_expr, warm_start, dict(fitargs))
     out = run_fits(sw.model, sw.tau[None, :], sw.Y, sw.W, sw.problems, sw.stages, sw.init, sw.lo, sw.hi,
-                   sw.options, gpu_id)
+                   sw.options, gpu_id, covariance=bool(return_model_results) and sw.calc_covar)
     if np.any(out["status"] == ST_NONFINITE):
         raise ValueError(NAN_MESSAGE)
     return _sweep_results(sw, out, bool(return_model_results))
@@ -414,7 +414,7 @@ def fit_multik_batch(jobs: Sequence[Dict[str, Any]], model: Model, *, warm_start
     W = np.concatenate(Ws) if Ws else None
     out = run_fits(sweeps[0].model, X, np.concatenate(Ys), W, np.concatenate(probs).astype(np.int32),
                    [st for st in stages if st], np.concatenate(inits), np.concatenate(los), np.concatenate(his),
-                   options, gpu_id)
+                   options, gpu_id, covariance=return_model_results)
     results = []
     for i, (sw, off) in enumerate(zip(sweeps, offsets)):
         n = sw.problems.shape[0]

@@ -370,7 +370,9 @@ int fddm_b200_experiment_dft_stage(int variant, const void* d_rows, uint64_t npa
    parameters; a
    chain also ends at an entry that is not a problem), and optionally the
    final residuals ([nproblems][m], the first mp of each row; d_residual may
-   be NULL).
+   be NULL) and the covariance of the parameters ([nproblems][nparams]
+   [nparams], scaled by chi^2 / nfree, zero rows and columns for fixed
+   parameters, NaN where it has no finite value; d_covar may be NULL).
    The workspace holds (2 + nparams) * m doubles per concurrently running
    chain; fddm_b200_fit_workspace_bytes gives the size that runs every chain
    at once (a smaller one runs fewer at a time, down to one). */
@@ -391,7 +393,8 @@ int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, uint64_t ldx, uin
                      const int32_t* d_chain_problems, uint64_t nchains, int nvary, const double* d_init,
                      const double* d_min, const double* d_max, const double* options, double* d_values,
                      double* d_stderr, double* d_chisqr, int32_t* d_nfev, int32_t* d_info, int32_t* d_status,
-                     double* d_residual, void* d_workspace, uint64_t workspace_bytes, void* stream);
+                     double* d_residual, double* d_covar, void* d_workspace, uint64_t workspace_bytes,
+                     void* stream);
 
 #ifdef __cplusplus
 }

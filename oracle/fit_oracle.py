@@ -265,13 +265,14 @@ def lm_fit(func, names: Sequence[str], params: Dict[str, dict], x: np.ndarray, y
         covar = None
     stderr = {p: None for p in names}
     if covar is not None:
-        covar = covar * redchi
+        covar = covar * redchi  # lmfit's result.covar (varying parameters, in order)
         for p in names:
             stderr[p] = 0.0
         for i, p in enumerate(var):
             stderr[p] = float(np.sqrt(covar[i, i]))
     return {"values": e, "stderr": stderr, "success": ier in (1, 2, 3, 4), "ier": int(ier),
-            "nfev": int(info["nfev"]), "chisqr": chisqr, "redchi": redchi, "residual": fvec, "aborted": False}
+            "nfev": int(info["nfev"]), "chisqr": chisqr, "redchi": redchi, "residual": fvec, "aborted": False,
+            "covar": covar, "var_names": var}
 
 
 def fit_multik(func, names: Sequence[str], params: Dict[str, dict], tau: np.ndarray, data: np.ndarray, ref: int,

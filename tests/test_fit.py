@@ -139,7 +139,8 @@ class FakeDevice:
         self.func, self.names, _ = fo.MODELS[model_name]
         self.launches = []
 
-    def __call__(self, model, x, Y, W, problems, stages, init, lo, hi, options, gpu_id=0, residual=False):
+    def __call__(self, model, x, Y, W, problems, stages, init, lo, hi, options, gpu_id=0, residual=False,
+                 covariance=False):
         P = len(init)
         npar = len(self.names)
         vals = np.full((P, npar), np.nan)

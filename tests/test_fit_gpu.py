@@ -149,6 +149,13 @@ def test_standard_errors_at_the_solution(name):
         os_, ds = ora["stderr"][p], dev.params[p].stderr
         if os_ is not None and np.isfinite(os_) and os_ > 0:
             assert abs(ds / os_ - 1) < 1e-4, (name, p, ds, os_)
+    # lmfit's covar and correlations: entries relative to sqrt(c_ii c_jj)
+    if ora["covar"] is not None and np.all(np.isfinite(ora["covar"])):
+        assert dev.var_names == ora["var_names"]
+        d = np.sqrt(np.outer(np.diag(ora["covar"]), np.diag(ora["covar"])))
+        assert np.max(np.abs(dev.covar - ora["covar"]) / d) < 1e-4, name
+        a, b = dev.var_names[0], dev.var_names[1]
+        assert abs(dev.params[a].correl[b] - ora["covar"][0, 1] / d[0, 1]) < 1e-4
 
 
 def test_fit_with_estimated_simple_parameters():
