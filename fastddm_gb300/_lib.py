@@ -129,8 +129,11 @@ _SIGNATURES = {
     "fddm_b200_fit_workspace_bytes": (ctypes.c_int, [ctypes.c_int, _u64, _u64, ctypes.POINTER(_u64)]),
     "fddm_b200_fit_lm": (
         ctypes.c_int,
+        # model, m, x, ldx, nx, y, ldy, ny, w, ldw, nw, problems, nproblems, chain offsets, chain problems,
+        # nchains, nvary, init, min, max, options, values, stderr, chisqr, nfev, info, status, residual,
+        # covar, workspace, workspace bytes, stream
         [ctypes.c_int, _u64, _vp, _u64, _u64, _vp, _u64, _u64, _vp, _u64, _u64, _vp, _u64, _vp, _vp, _u64,
-         ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u64, _vp],
+         ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u64, _vp],
     ),
     "fddm_b200_tiff_info": (
         ctypes.c_int,

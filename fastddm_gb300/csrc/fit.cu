@@ -62,6 +62,9 @@ extern "C" int fddm_b200_fit_lm(int model, uint64_t m, const double* d_x, uint64
       nw > (1ull << 30) || nx > (1ull << 30))
     return fail_with(FDDM_ERR_UNSUPPORTED, "too many data points, problems or chains");
   if (!options) return fail_with(FDDM_ERR_INVALID, "null options");
+  // every iteration evaluates the model, so max_nfev bounds a fit's run; above this a fit that never
+  // converges could hold the GPU for minutes
+  if (!(options[5] <= 1e6)) return fail_with(FDDM_ERR_UNSUPPORTED, "max_nfev above 1,000,000");
   if (nchains == 0 || nproblems == 0) return FDDM_OK;
   if (!d_x || !d_y || !d_problems || !d_chain_offsets || !d_chain_problems || !d_init || !d_min || !d_max ||
       !d_values || !d_stderr || !d_chisqr || !d_nfev || !d_info || !d_status || !d_workspace)

@@ -357,7 +357,8 @@ int fddm_b200_experiment_dft_stage(int variant, const void* d_rows, uint64_t npa
    when there are at most two chains per SM; chains run concurrently.
    d_init, d_min, d_max, d_values, d_stderr: [nproblems][nparams] doubles.
    options (host, 6 doubles): ftol, xtol, gtol, epsfcn, factor, max_nfev
-   (<= 0: 2000*(nvary+1)); lmfit's defaults are 1e-7, 1e-7, 1e-7, 0, 100, 0.
+   (<= 0: 2000*(nvary+1); above 1,000,000: FDDM_ERR_UNSUPPORTED); lmfit's
+   defaults are 1e-7, 1e-7, 1e-7, 0, 100, 0.
    Outputs per problem: fitted values (fixed parameters keep theirs),
    standard errors (0 for fixed parameters; NaN where the covariance has
    entries that are not finite, e.g. a parameter exactly on a bound; -1 for

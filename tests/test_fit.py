@@ -307,3 +307,32 @@ def test_fit_multik_batch_gives_each_job_its_own_result(monkeypatch):
             np.testing.assert_array_equal(tb[col], ta[col], err_msg=col)
     with pytest.raises(ValueError, match="same number"):
         gfit.fit_multik_batch([dict(data=a1, ref=4), dict(data=a2, ref=9, fixed_params={"B": B2})], m)
+
+
+def test_fit_abi_refuses_bad_arguments_without_device_work(built_lib):
+    """Argument checks of fddm_b200_fit_lm that return before any device work (CPU)."""
+    import ctypes
+
+    lib = built_lib
+    u64 = ctypes.c_uint64
+    nb = u64(0)
+    assert lib.fddm_b200_fit_model_nparams(3) == 4 and lib.fddm_b200_fit_model_nparams(99) == 0
+    assert lib.fddm_b200_fit_workspace_bytes(99, 10, 1, ctypes.byref(nb)) == 1
+    opts = np.array([1e-7, 1e-7, 1e-7, 0.0, 100.0, 0.0])
+    args = dict(m=10, nx=1, ny=1, nw=0, nprob=1, nch=1, nvary=3)
+
+    def call(model=3, opts=opts, **kw):
+        a = dict(args, **kw)
+        dummy = ctypes.c_void_p(16)  # never dereferenced: every case fails its checks first
+        return lib.fddm_b200_fit_lm(model, a["m"], dummy, a["m"], a["nx"], dummy, a["m"], a["ny"], None, 0, a["nw"],
+                                    dummy, a["nprob"], dummy, dummy, a["nch"], a["nvary"], dummy, dummy, dummy,
+                                    opts.ctypes.data, dummy, dummy, dummy, dummy, dummy, dummy, None, None,
+                                    dummy, 1 << 20, None)
+
+    assert call(model=99) == 1                 # unknown model
+    assert call(nvary=5) == 1                  # more varying parameters than the model has
+    assert call(m=2) == 1                      # fewer points than varying parameters
+    big = opts.copy()
+    big[5] = 1e7
+    assert call(opts=big) == 4                 # max_nfev above the limit
+    assert "max_nfev" in lib.fddm_b200_last_error().decode()

@@ -283,3 +283,21 @@ def test_fit_multik_batch_matches_single_calls():
         for p in ("A", "Gamma"):
             tol = np.maximum(PAR_TOL * np.abs(ta[p]), SE_FRAC * ta[f"{p}_stderr"])
             assert np.all(np.abs(tb[p] - ta[p]) <= tol), p
+
+
+def test_fit_on_a_side_stream_equals_the_default_stream():
+    """The fit launches on the caller's current stream (a non-zero stream handle crosses the C ABI)."""
+    import torch
+
+    from fastddm_gb300 import fit_models
+
+    m = fit_models.simple_exponential_model
+    x, y = _curve("simple_exponential_model", 3)
+    p = m.make_params(**CASES["simple_exponential_model"][1])
+    ref = m.fit(y, params=p, x=x)
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        got = m.fit(y, params=p, x=x)
+    for n in m.param_names:
+        assert got.params[n].value == ref.params[n].value
+    assert got.chisqr == ref.chisqr and got.nfev == ref.nfev

@@ -140,3 +140,21 @@ def test_lag_zero_warning_before_device():
         except RuntimeError:
             pass  # no GPU in this process
     assert any("Found 0 in lags" in str(x.message) for x in w)
+
+
+def test_bindings_match_the_header_declarations():
+    """Every ctypes binding has as many arguments as its C declaration: a missing one would send the
+    trailing arguments (the stream) through ctypes' default int conversion."""
+    import re
+
+    from fastddm_gb300 import _lib
+
+    text = (ROOT / "include" / "fddm_b200.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    decls = {}
+    for m in re.finditer(r"\b(fddm_b200_\w+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+        params = " ".join(m.group(2).split())
+        decls[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    for name, (_, argtypes) in _lib._SIGNATURES.items():
+        assert name in decls, name
+        assert len(argtypes) == decls[name], (name, len(argtypes), decls[name])
