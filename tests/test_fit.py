@@ -148,6 +148,7 @@ class FakeDevice:
         out = {"values": vals, "stderr": se, "chisqr": np.zeros(P), "nfev": np.zeros(P, np.int32),
                "info": np.zeros(P, np.int32), "status": np.zeros(P, np.int32),
                "nvary": bin(int(problems[0][3])).count("1"), "device_ms": 0.0, "launches": len(stages)}
+        self.problems = np.array(problems)
         done = set()
         for chains in stages:
             self.launches.append([list(c) for c in chains])
@@ -336,3 +337,27 @@ def test_fit_abi_refuses_bad_arguments_without_device_work(built_lib):
     big[5] = 1e7
     assert call(opts=big) == 4                 # max_nfev above the limit
     assert "max_nfev" in lib.fddm_b200_last_error().decode()
+
+
+def test_fit_multik_host_options(monkeypatch):
+    """calc_covar, scale_covar, a user weights array shared by every k, and lmfit's warning for
+    keyword arguments that are not the model's."""
+    aa, (A, B, G) = synthetic_aa(K=8, seed=7)
+    m = fit_models.simple_exponential_model
+    fake = FakeDevice("simple_exponential_model")
+    monkeypatch.setattr(gfit, "run_fits", fake)
+    base, _ = gfit.fit_multik(aa, m, 3, A=A[3], B=B[3], Gamma=G[3])
+    nocov, _ = gfit.fit_multik(aa, m, 3, A=A[3], B=B[3], Gamma=G[3], calc_covar=False)
+    assert np.all(np.isnan(nocov["A_stderr"])) and np.array_equal(nocov["A"], base["A"])
+    unscaled, mres = gfit.fit_multik(aa, m, 3, A=A[3], B=B[3], Gamma=G[3], scale_covar=False,
+                                     return_model_results=True)
+    red = np.array([r.redchi for r in mres])
+    np.testing.assert_allclose(unscaled["Gamma_stderr"], base["Gamma_stderr"] / np.sqrt(red), rtol=1e-12)
+    assert np.all(unscaled["beta_stderr"] == 0.0)  # fixed: 0, not divided
+    w = 1.0 / (1.0 + np.arange(aa.tau.size))
+    with pytest.warns(UserWarning, match="does not match"):
+        weighted, _ = gfit.fit_multik(aa, m, 3, A=A[3], B=B[3], Gamma=G[3], weights=w, bogus=1)
+    assert np.all(fake.problems[:, 1] == 0)  # every fit, the first at ref included, reads the weights row
+    assert not np.array_equal(weighted["Gamma"], base["Gamma"])
+    with pytest.raises(ValueError, match="warm_start"):
+        gfit.fit_multik(aa, m, 3, warm_start="sideways")
