@@ -301,3 +301,45 @@ def test_fit_on_a_side_stream_equals_the_default_stream():
     for n in m.param_names:
         assert got.params[n].value == ref.params[n].value
     assert got.chisqr == ref.chisqr and got.nfev == ref.nfev
+
+
+def test_pipeline_ddm_azimuthal_average_fit():
+    """DDM of a drift-free Brownian scene, its azimuthal average, the polyfit noise estimate and the
+    reference's sweep (set up as fit.py's docstring does) against the oracle's sweep on the same
+    average: parameters within tolerance on every k the oracle determines well, success flags equal."""
+    import copy
+
+    import fastddm_gb300 as fddm
+    from fastddm_gb300 import fit as gfit
+    from fastddm_gb300 import fit_models, noise_est
+    from fastddm_gb300.synthetic import Scene, make_stack
+
+    # D = 0.05 px^2/frame and k up to 1.5: Gamma = D k^2 up to ~0.1/frame, resolved by lags 1..255
+    imgs = make_stack(Scene(256, 128, 128, 300, 2.0, 2000.0, 0.05, 500.0, 0.0, "uint16", 3))
+    lags = np.arange(1, 256)
+    sf = fddm.ddm(imgs, lags, mode="fft")
+    aa = fddm.azimuthal_average(sf, bins=32, range=(0.0, 1.5))
+    a = copy.copy(aa)
+    data = a._data.copy()
+    data[~np.all(np.isfinite(a.err) & (a.err > 0), axis=1), 0] = np.nan  # the one-pixel k = 0 bin
+    a._data = data
+    B, _ = noise_est.estimate_camera_noise(a, mode="polyfit")
+    valid = np.flatnonzero(~np.isnan(a.data[:, 0]))
+    ref = int(valid[len(valid) // 4])
+    A0 = 2.0 * a.var[ref] - B[ref]
+    G0 = 1.0 / a.tau[int(np.argmin(np.abs((a.data[ref] - B[ref]) / A0 - 0.5)))]
+    table, _ = gfit.fit_multik(a, fit_models.simple_exponential_model, ref, A=A0, B=B[ref], Gamma=G0,
+                               use_err=True)
+    params = fo.make_params("simple_exponential_model")
+    params["A"]["value"], params["B"]["value"], params["Gamma"]["value"] = A0, B[ref], G0
+    want = fo.fit_multik(fo.MODELS["simple_exponential_model"][0], ["A", "B", "Gamma", "beta"], params, a.tau,
+                         a.data, ref, err=a.err, use_err=True)
+    np.testing.assert_array_equal(table["success"], want["success"])
+    with np.errstate(invalid="ignore", divide="ignore"):
+        rel = np.maximum(want["A_stderr"] / np.abs(want["A"]), want["Gamma_stderr"] / np.abs(want["Gamma"]))
+    wd = ~np.isnan(want["A"]) & want["success"] & np.isfinite(rel) & (rel < 0.1)
+    assert wd.sum() >= 8  # enough well-determined k for the comparison to mean something
+    for n in ("A", "B", "Gamma"):
+        scale = np.abs(want["A"][wd]) if n == "B" else np.abs(want[n][wd])
+        tol = np.maximum(PAR_TOL * scale, SE_FRAC * want[f"{n}_stderr"][wd])
+        assert np.all(np.abs(table[n][wd] - want[n][wd]) <= tol), n
