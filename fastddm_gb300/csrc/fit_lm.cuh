@@ -279,7 +279,7 @@ struct Batch {
 template <int NV, int W>
 struct Fit {
   const Batch& b;
-  Grp<W>& G;
+  Grp<W> G;  // a copy: each fit ends with a group barrier, so its sums may start from either buffer
   const double* x;  // this problem's abscissae, m of them
   const double* y;
   const double* w;
@@ -347,8 +347,10 @@ __device__ void qr_pivot(Fit<NV, W>& F, const double (&colsq)[NV], double* wt, d
   constexpr int S = 32 * W;
   double rdiag[NV], wa[NV];
   bool recomp[NV];
+  double* pc[NV];  // column at pivot position k (kept in registers: swapped with ipvt, indexed statically)
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
+    pc[k] = F.fj[k];
     ipvt[k] = k;
     acnorm[k] = sqrt(colsq[k]);
     rdiag[k] = acnorm[k];
@@ -369,7 +371,7 @@ __device__ void qr_pivot(Fit<NV, W>& F, const double (&colsq)[NV], double* wt, d
         if (i < j) continue;
 #pragma unroll
         for (int k = j; k < NV; ++k) {
-          const double v = F.fj[ipvt[k]][i];
+          const double v = pc[k][i];
           part[k - j] = __fma_rn(v, v, part[k - j]);
         }
       }
@@ -377,7 +379,7 @@ __device__ void qr_pivot(Fit<NV, W>& F, const double (&colsq)[NV], double* wt, d
     for (int k = 0; k <= NV; ++k) bv[k] = 0.0;
     if (tid == j) {
 #pragma unroll
-      for (int k = j; k < NV; ++k) bv[k - j] = F.fj[ipvt[k]][j];
+      for (int k = j; k < NV; ++k) bv[k - j] = pc[k][j];
       bv[NV - j] = wt[j];
     }
     bool nf = false;
@@ -406,6 +408,7 @@ __device__ void qr_pivot(Fit<NV, W>& F, const double (&colsq)[NV], double* wt, d
       for (int k = j + 1; k < NV; ++k)
         if (k == kmax) {
           int ti = ipvt[j]; ipvt[j] = ipvt[k]; ipvt[k] = ti;
+          double* tp = pc[j]; pc[j] = pc[k]; pc[k] = tp;
           double t = fresh[j]; fresh[j] = fresh[k]; fresh[k] = t;
           t = rowj[j]; rowj[j] = rowj[k]; rowj[k] = t;
           rdiag[k] = rdiag[j];
@@ -419,7 +422,7 @@ __device__ void qr_pivot(Fit<NV, W>& F, const double (&colsq)[NV], double* wt, d
       if (rowj[j] < 0.0) ajnorm = -ajnorm;
       const double rn = 1.0 / ajnorm;
       const double vjj = rowj[j] * rn + 1.0;
-      double* cj = F.fj[ipvt[j]];
+      double* cj = pc[j];
       double dot[NV];  // dot[0]: with wt; dot[k - j]: with column k > j
 #pragma unroll
       for (int k = 0; k < NV; ++k) dot[k] = 0.0;
@@ -430,7 +433,7 @@ __device__ void qr_pivot(Fit<NV, W>& F, const double (&colsq)[NV], double* wt, d
         cj[i] = v;
         dot[0] = __fma_rn(v, wt[i], dot[0]);
 #pragma unroll
-        for (int k = j + 1; k < NV; ++k) dot[k - j] = __fma_rn(v, F.fj[ipvt[k]][i], dot[k - j]);
+        for (int k = j + 1; k < NV; ++k) dot[k - j] = __fma_rn(v, pc[k][i], dot[k - j]);
       }
       double none[1];
       F.G.sum(dot, NV - j, nf, none, 0, -1);
@@ -444,7 +447,7 @@ __device__ void qr_pivot(Fit<NV, W>& F, const double (&colsq)[NV], double* wt, d
         const double v = cj[i];
         wt[i] = __fma_rn(v, tw, wt[i]);
 #pragma unroll
-        for (int k = j + 1; k < NV; ++k) F.fj[ipvt[k]][i] = __fma_rn(-tk[k], v, F.fj[ipvt[k]][i]);
+        for (int k = j + 1; k < NV; ++k) pc[k][i] = __fma_rn(-tk[k], v, pc[k][i]);
       }
       qtf[j] = __fma_rn(vjj, tw, wj);
 #pragma unroll
@@ -924,7 +927,9 @@ __device__ void run_problem(const Batch& b, int prob, double* slot, Grp<W>& G) {
 
 // W = 1: each warp of the CTA runs its own chains; W = 4: the CTA runs one chain at a time.
 template <int NV, int W>
-__global__ void __launch_bounds__(32 * kWarpsPerCta) k_fit_lm(Batch b) {
+// __grid_constant__: the fits keep references to the batch description, which then stay in the
+// parameter space instead of a per-thread copy in local memory
+__global__ void __launch_bounds__(32 * kWarpsPerCta) k_fit_lm(const __grid_constant__ Batch b) {
   static_assert(W == 1 || W == kWarpsPerCta, "a group is one warp or the whole CTA");
   __shared__ double red[2 * kMaxW * kMaxP];
   __shared__ int flags[2 * kMaxW];
