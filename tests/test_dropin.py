@@ -2,7 +2,7 @@
 
 Applies the two edits a FastDDM maintainer makes to bind the core (the
 ``'b200'`` rule in ``_fftopt.next_fast_len``, ``_backend['b200']`` in
-``_ddm``; INTEGRATION.md section 2) to the reference's Python package imported
+``_ddm``) to the reference's Python package imported
 in-process, then calls the reference's ``fastddm.ddm(..., core='b200')``.  The
 device computation behind ``ddm_fft_b200`` / ``ddm_diff_b200`` is replaced by
 the FP64 oracle (there is no GPU here), so what this checks is the boundary:
