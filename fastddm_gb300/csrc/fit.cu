@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <algorithm>
+#include <cstdlib>
 #include <string>
 #include "fddm_b200.h"
 #include "fddm_internal.h"
@@ -20,10 +21,17 @@ int sm_count() {
   return nsm > 0 ? nsm : 152;
 }
 
-// Warps per chain: with at most two chains per SM a chain takes a whole CTA (its per-point work
-// spread over the SM's four sub-partitions, which one warp per chain would mostly leave idle); with
-// more, each warp runs its own chains (no sub-partition repeats the small-matrix work of another).
-int group_warps(uint64_t nchains) { return nchains <= 2 * (uint64_t)sm_count() ? fddm::fitlm::kWarpsPerCta : 1; }
+// Warps per chain: with at most four chains per SM a chain takes a whole CTA (its per-point work
+// spread over the SM's four sub-partitions; measured faster up to 512 chains of one fit each, whose
+// few long fits set the launch's time); with more, each warp runs its own chains (no sub-partition
+// repeats the small-matrix work of another).  FDDM_B200_FIT_GROUP_WARPS=1|4 overrides the choice
+// (tuning runs).
+int group_warps(uint64_t nchains) {
+  const char* v = std::getenv("FDDM_B200_FIT_GROUP_WARPS");
+  const int x = v ? std::atoi(v) : 0;
+  if (x == 1 || x == fddm::fitlm::kWarpsPerCta) return x;
+  return nchains <= 4 * (uint64_t)sm_count() ? fddm::fitlm::kWarpsPerCta : 1;
+}
 
 // groups resident at once (8 CTAs per SM)
 uint64_t max_slots(int group) { return (uint64_t)sm_count() * 8 * (fddm::fitlm::kWarpsPerCta / group); }

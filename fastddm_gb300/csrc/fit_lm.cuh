@@ -20,7 +20,7 @@
 // Layout.  A group of threads runs one chain of fits (a fit_multik sweep
 // warm-starts each fit from the previous result, so a chain is sequential):
 // one warp when there are many chains, or the W = 4 warps of a CTA when there
-// are at most two chains per SM, so that the per-point work of a chain is
+// are at most four chains per SM, so that the per-point work of a chain is
 // spread over the four sub-partitions of its SM (on GB300 an FP64 instruction
 // occupies a sub-partition's FP64 pipe for about 64 cycles whatever the
 // number of active lanes, and a single chain is bound by that latency).  The

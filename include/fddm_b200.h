@@ -354,7 +354,7 @@ int fddm_b200_experiment_dft_stage(int variant, const void* d_rows, uint64_t npa
    earlier call.  Starting values are clipped into [min, max] as lmfit does.
    Chains: chain c runs problems d_chain_problems[d_chain_offsets[c] ..
    d_chain_offsets[c+1]-1] in order on one warp, or on a CTA of four warps
-   when there are at most two chains per SM; chains run concurrently.
+   when there are at most four chains per SM; chains run concurrently.
    d_init, d_min, d_max, d_values, d_stderr: [nproblems][nparams] doubles.
    options (host, 6 doubles): ftol, xtol, gtol, epsfcn, factor, max_nfev
    (<= 0: 2000*(nvary+1); above 1,000,000: FDDM_ERR_UNSUPPORTED); lmfit's

@@ -259,7 +259,8 @@ def test_evaluation_limit_stops_the_fit():
 
 def test_fit_multik_batch_matches_single_calls():
     """Three datasets of different sizes in one batch (six sweeps, a CTA each, as in single calls):
-    bit-identical to fit_multik on each; 200 datasets (400 sweeps, a warp each): within tolerance."""
+    bit-identical to fit_multik on each; 320 datasets (640 sweeps: more than four per SM, a warp
+    each): within tolerance."""
     from fastddm_gb300 import fit as gfit
     from fastddm_gb300 import fit_models
 
@@ -273,7 +274,7 @@ def test_fit_multik_batch_matches_single_calls():
         ta, _ = gfit.fit_multik(job["data"], m, job["ref"], **kw)
         for col in ta.columns:
             np.testing.assert_array_equal(tb[col], ta[col], err_msg=col)
-    many = [_aa(K=24, m=50 + (s % 7) * 10, seed=100 + s) for s in range(200)]
+    many = [_aa(K=24, m=50 + (s % 7) * 10, seed=100 + s) for s in range(320)]
     jobs = [dict(data=a, ref=8, A=A[8], B=B[8], Gamma=G[8], use_err=True) for a, (A, B, G) in many]
     batch = gfit.fit_multik_batch(jobs, m)
     for job, (tb, _) in zip(jobs[:10], batch[:10]):
