@@ -25,8 +25,9 @@ returns a pandas DataFrame.  Neither lmfit nor pandas is installed here, so:
   parameters, None without a covariance).
 
 Parity against lmfit's own outputs is therefore unpinned; the MINPACK core is
-pinned by the known-answer tests in ``tests/test_fit.py`` (the reference has
-no test or golden output for fitting).
+pinned by the known-answer tests in ``tests/test_fit.py`` (among them the
+published minima of MINPACK's test set), the reference having no test or
+golden output for fitting.
 """
 
 from __future__ import annotations

@@ -44,6 +44,38 @@ def test_oracle_linear_least_squares_known_answer():
     assert abs(r["stderr"]["c1"] / np.sqrt(cov[1, 1]) - 1) < 1e-6
 
 
+@pytest.mark.parametrize("case", ["bard", "kowalik_osborne", "meyer", "beale"])
+def test_oracle_moré_garbow_hillstrom_known_answers(case):
+    """Problems of the MINPACK test set (Moré, Garbow and Hillstrom, ACM TOMS 7, 1981) from their
+    standard starting points: the minimum sums of squares they publish."""
+    if case == "bard":
+        y = np.array([0.14, 0.18, 0.22, 0.25, 0.29, 0.32, 0.35, 0.39, 0.37, 0.58, 0.73, 0.96, 1.34, 2.10, 4.39])
+        u = np.arange(1, 16)
+        v, w = 16 - u, np.minimum(u, 16 - u)
+        func, names, start, want = (lambda x, a, b, c: a + u / (b * v + c * w)), list("abc"), (1, 1, 1), 8.21487e-3
+    elif case == "kowalik_osborne":
+        y = np.array([0.1957, 0.1947, 0.1735, 0.1600, 0.0844, 0.0627, 0.0456, 0.0342, 0.0323, 0.0235, 0.0246])
+        u = np.array([4.0, 2.0, 1.0, 0.5, 0.25, 0.167, 0.125, 0.1, 0.0833, 0.0714, 0.0625])
+        func = lambda x, a, b, c, d: a * (u ** 2 + u * b) / (u ** 2 + u * c + d)
+        names, start, want = list("abcd"), (0.25, 0.39, 0.415, 0.39), 3.07505e-4
+    elif case == "meyer":
+        y = np.array([34780, 28610, 23650, 19630, 16370, 13720, 11540, 9744, 8261, 7030, 6005, 5147, 4427, 3820,
+                      3307, 2872], float)
+        t = 45.0 + 5.0 * np.arange(1, 17)
+        func, names, start, want = (lambda x, a, b, c: a * np.exp(b / (t + c))), list("abc"), (0.02, 4000, 250), 87.9458
+    else:  # beale: minimum 0 at (3, 0.5)
+        y = np.array([1.5, 2.25, 2.625])
+        func = lambda x, a, b: np.array([a * (1 - b), a * (1 - b * b), a * (1 - b ** 3)])
+        names, start, want = list("ab"), (1.0, 1.0), 0.0
+    par = {n: {"value": float(v)} for n, v in zip(names, start)}
+    r = fo.lm_fit(func, names, par, np.zeros(y.size), y)
+    assert r["success"]
+    if want == 0.0:
+        assert r["chisqr"] < 1e-20 and abs(r["values"]["a"] - 3.0) < 1e-8 and abs(r["values"]["b"] - 0.5) < 1e-8
+    else:
+        assert abs(r["chisqr"] / want - 1) < 1e-5, r["chisqr"]
+
+
 def test_oracle_bound_is_respected():
     """A parameter whose unconstrained optimum lies below its lower bound ends on the bound."""
     x = np.linspace(0, 4, 30)
